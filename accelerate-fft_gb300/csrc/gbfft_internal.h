@@ -1,0 +1,83 @@
+// Internal declarations shared by the host planner and the device kernels.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace gbfft {
+
+constexpr int kMaxStages = 16;
+
+// Largest transform length one CTA computes in shared memory (two ping-pong
+// buffers of one column each); longer axes are split four-step.
+constexpr int kCapC32 = 8192;
+constexpr int kCapC64 = 4096;
+
+// Pre- and post-operations fused into a pencil pass.
+enum PassFlags : uint32_t {
+  F_CONJ_IN = 1u << 0,     // conjugate every loaded element (backward via forward)
+  F_CONJ_OUT = 1u << 1,    // conjugate every stored element
+  F_SCALE = 1u << 2,       // multiply stored elements by `scale` (Inverse 1/N)
+  F_TW4 = 1u << 3,         // four-step twiddle W_N^{e*k} on store
+  F_TW4_BATCH = 1u << 4,   //   ... exponent multiplier e = batch index (else column)
+  F_CHIRP_IN = 1u << 5,    // x[l] * chirp[l] on load (l = logical input index)
+  F_PAD_IN = 1u << 6,      // zero for logical input index l >= n_in
+  F_BLUE = 1u << 7,        // in-kernel Bluestein: filter, inverse, chirp on store
+  F_FILTER_OUT = 1u << 8,  // multiply by filter[l] then conjugate, on store
+  F_CHIRP_OUT = 1u << 9,   // conjugate then multiply by chirp[l] on store
+  F_TRUNC_OUT = 1u << 10,  // store only logical output index l < n_out
+};
+
+struct StageInfo {
+  int radix;   // 2, 3, 4, 5, 7, 8 or 16
+  int ns;      // product of the radices of earlier stages (Stockham Ns)
+  int tw_off;  // offset of this stage's twiddles in the stage table
+};
+
+// One pencil pass: for each (batch b, column c) transform the pencil
+// i -> base + b_lo*bs + b_hi*bs2 + c*cs + i*es of length n, in shared
+// memory, where b = b_hi*nb_lo + b_lo.
+struct PassDesc {
+  const void* in;
+  void* out;
+  int64_t in_es, in_cs, in_bs, in_bs2;
+  int64_t out_es, out_cs, out_bs, out_bs2;
+  int64_t ncols;   // columns per batch
+  int64_t nbatch;  // batches (nb_lo * number of b_hi)
+  int64_t nb_lo;   // extent of the inner batch index
+  int n;           // transform length computed in shared memory
+  int W;           // columns per CTA tile
+  int pitch;       // shared-memory column pitch (elements, odd)
+  int threads;     // CTA size
+  int nstages;
+  int load_cfast;   // 1: loads map consecutive threads to consecutive columns
+  int store_cfast;  // 1: stores map consecutive threads to consecutive columns
+  uint32_t flags;
+  StageInfo st[kMaxStages];
+  const void* tw;  // stage twiddles (element type of the pass)
+  double scale;
+  // logical index used by chirp / pad / filter / truncation:
+  //   l_in = i*lin_es + c*lin_cs,  l_out = k*lout_es + c*lout_cs
+  int64_t lin_es, lin_cs, lout_es, lout_cs;
+  int64_t n_in, n_out;
+  // four-step twiddle W_N^t, t = (e*k) mod N, W = hi[t >> shift] * lo[t & mask]
+  int64_t tw4_n;
+  int tw4_shift;
+  const void* tw4_lo;
+  const void* tw4_hi;
+  const void* chirp;   // Bluestein chirp c[l] = exp(-i*pi*l^2/n), l < n
+  const void* filter;  // Bluestein filter spectrum DFT(conj chirp)/m, length m
+};
+
+size_t pass_smem_bytes(const PassDesc& d, bool is_double);
+int pass_grid(const PassDesc& d);
+
+// Launch one pencil pass on `stream`; returns a cudaError_t.
+cudaError_t launch_pass(const PassDesc& d, bool is_double, cudaStream_t stream);
+
+// Prepare kernel attributes (max dynamic shared memory); idempotent.
+cudaError_t prepare_kernels();
+
+}  // namespace gbfft

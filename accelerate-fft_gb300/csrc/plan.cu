@@ -1,0 +1,860 @@
+// Host side of the engine: factoriser, twiddle / Bluestein table builder,
+// pass sequencing, the per-context plan cache and the C ABI of gbfft.h.
+//
+// Replaces, on the accelerate-fft side (paths in the accelerate-fft tree):
+//   cufftPlan1d/2d/3d/Many constructors ... src/Data/Array/Accelerate/Math/FFT/LLVM/PTX.hs:137-170
+//   withPlan / Plans cache ............... src/Data/Array/Accelerate/Math/FFT/LLVM/PTX/Plans.hs:40-90
+//   setStream + execC2C/execZ2Z .......... PTX.hs:112-124
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "gbfft.h"
+#include "gbfft_internal.h"
+#include "plan_internal.h"
+
+namespace gbfft {
+
+// ---------------------------------------------------------------------------
+// exact unit roots
+cd unit_root(int64_t t, int64_t L) {
+  t %= L;
+  if (t < 0) t += L;
+  // angle = 2*pi*t/L = q*pi/2 + (pi/2)*(r/L), q = floor(4t/L)
+  const int64_t q = (4 * t) / L;
+  const int64_t r = 4 * t - q * L;
+  const double hp = 1.57079632679489661923132169163975;
+  double c, s;
+  if (2 * r <= L) {
+    const double x = hp * double(r) / double(L);
+    c = std::cos(x);
+    s = std::sin(x);
+  } else {
+    const double x = hp * double(L - r) / double(L);
+    c = std::sin(x);
+    s = std::cos(x);
+  }
+  double c2 = c, s2 = s;
+  switch (q & 3) {
+    case 1: c2 = -s; s2 = c; break;
+    case 2: c2 = -c; s2 = -s; break;
+    case 3: c2 = s; s2 = -c; break;
+    default: break;
+  }
+  return cd(c2, -s2);  // exp(-i * angle)
+}
+
+bool factor_device(int64_t n, std::vector<int>& out) {
+  out.clear();
+  if (n < 1) return false;
+  int64_t m = n;
+  int a2 = 0, a3 = 0, a5 = 0, a7 = 0;
+  while (m % 2 == 0) { m /= 2; ++a2; }
+  while (m % 3 == 0) { m /= 3; ++a3; }
+  while (m % 5 == 0) { m /= 5; ++a5; }
+  while (m % 7 == 0) { m /= 7; ++a7; }
+  if (m != 1) return false;
+  while (a2 >= 4) { out.push_back(16); a2 -= 4; }
+  if (a2 == 3) out.push_back(8);
+  else if (a2 == 2) out.push_back(4);
+  else if (a2 == 1) out.push_back(2);
+  for (int i = 0; i < a7; ++i) out.push_back(7);
+  for (int i = 0; i < a5; ++i) out.push_back(5);
+  for (int i = 0; i < a3; ++i) out.push_back(3);
+  return true;
+}
+
+bool is_fast_length(int64_t n) {
+  std::vector<int> f;
+  return factor_device(n, f);
+}
+
+// FP64 Stockham FFT on the host (forward sign) for 7-smooth lengths; used
+// only at plan time for Bluestein filter spectra.
+void host_fft_fp64(std::vector<cd>& x) {
+  const int64_t n = int64_t(x.size());
+  if (n <= 1) return;
+  std::vector<int> f;
+  {
+    int64_t m = n;
+    while (m % 4 == 0) { f.push_back(4); m /= 4; }
+    while (m % 2 == 0) { f.push_back(2); m /= 2; }
+    while (m % 3 == 0) { f.push_back(3); m /= 3; }
+    while (m % 5 == 0) { f.push_back(5); m /= 5; }
+    while (m % 7 == 0) { f.push_back(7); m /= 7; }
+  }
+  std::vector<cd> roots(static_cast<size_t>(n));
+  for (int64_t t = 0; t < n; ++t) roots[size_t(t)] = unit_root(t, n);
+  std::vector<cd> y(static_cast<size_t>(n));
+  int64_t Ns = 1;
+  for (int R : f) {
+    const int64_t nb = n / R, step = n / (Ns * R);
+    for (int64_t j = 0; j < nb; ++j) {
+      const int64_t p = j % Ns;
+      cd v[7];
+      for (int r = 0; r < R; ++r) v[r] = x[size_t(j + r * nb)] * roots[size_t((p * r * step) % n)];
+      const int64_t base = (j - p) * R + p;
+      for (int k = 0; k < R; ++k) {
+        cd acc(0, 0);
+        for (int r = 0; r < R; ++r) acc += v[r] * roots[size_t(((r * k) % R) * nb)];
+        y[size_t(base + k * Ns)] = acc;
+      }
+    }
+    std::swap(x, y);
+    Ns *= R;
+  }
+}
+
+// Bluestein padded length: the 7-smooth m >= 2n-1 with the fewest
+// (stages + 1) * m among candidates up to the next power of two.
+int64_t bluestein_length(int64_t n) {
+  const int64_t lo = 2 * n - 1;
+  int64_t p2 = 1;
+  while (p2 < lo) p2 *= 2;
+  int64_t best = p2;
+  std::vector<int> f;
+  factor_device(p2, f);
+  double best_cost = double(p2) * double(f.size() + 1);
+  for (int64_t m = lo; m < p2; ++m) {
+    if (!factor_device(m, f)) continue;
+    const double cost = double(m) * double(f.size() + 1);
+    if (cost < best_cost) {
+      best_cost = cost;
+      best = m;
+    }
+  }
+  return best;
+}
+
+// ---------------------------------------------------------------------------
+size_t Builder::add(const std::vector<cd>& v) {
+  const size_t eb = dbl ? 16 : 8;
+  size_t off = (blob.size() + 255) & ~size_t(255);
+  blob.resize(off + v.size() * eb);
+  unsigned char* p = blob.data() + off;
+  for (size_t i = 0; i < v.size(); ++i) {
+    if (dbl) {
+      double t[2] = {v[i].real(), v[i].imag()};
+      std::memcpy(p + i * 16, t, 16);
+    } else {
+      float t[2] = {float(v[i].real()), float(v[i].imag())};
+      std::memcpy(p + i * 8, t, 8);
+    }
+  }
+  return off;
+}
+
+// Stage list + stage twiddle table for a shared-memory transform of length n.
+bool Builder::stages_for(int n, PassSpec& ps) {
+  std::vector<int> f;
+  if (!factor_device(n, f) || int(f.size()) > kMaxStages) return false;
+  auto it = stage_cache.find(n);
+  std::vector<int> offs(f.size());
+  if (it == stage_cache.end()) {
+    std::vector<cd> t;
+    int64_t Ns = 1;
+    for (size_t s = 0; s < f.size(); ++s) {
+      offs[s] = int(t.size());
+      const int R = f[s];
+      for (int64_t p = 0; p < Ns; ++p)
+        for (int r = 1; r < R; ++r) t.push_back(unit_root(p * r, Ns * R));
+      Ns *= R;
+    }
+    if (t.empty()) t.push_back(cd(1, 0));
+    StageTable st;
+    st.off = add(t);
+    st.offs = offs;
+    it = stage_cache.emplace(n, st).first;
+  }
+  ps.tw_off = int64_t(it->second.off);
+  ps.d.n = n;
+  ps.d.nstages = int(f.size());
+  int Ns = 1;
+  for (size_t s = 0; s < f.size(); ++s) {
+    ps.d.st[s].radix = f[s];
+    ps.d.st[s].ns = Ns;
+    ps.d.st[s].tw_off = it->second.offs[s];
+    Ns *= f[s];
+  }
+  return true;
+}
+
+void Builder::tw4_for(int64_t N, PassSpec& ps) {
+  int shift = 0;
+  while ((int64_t(1) << (2 * shift)) < N) ++shift;
+  auto it = tw4_cache.find(N);
+  if (it == tw4_cache.end()) {
+    const int64_t B = int64_t(1) << shift;
+    std::vector<cd> lo(static_cast<size_t>(B)), hi(static_cast<size_t>((N + B - 1) / B));
+    for (int64_t t = 0; t < B; ++t) lo[size_t(t)] = unit_root(t, N);
+    for (int64_t t = 0; t < int64_t(hi.size()); ++t) hi[size_t(t)] = unit_root(t * B, N);
+    Tw4 tw;
+    tw.lo = add(lo);
+    tw.hi = add(hi);
+    tw.shift = shift;
+    it = tw4_cache.emplace(N, tw).first;
+  }
+  ps.tw4lo_off = int64_t(it->second.lo);
+  ps.tw4hi_off = int64_t(it->second.hi);
+  ps.d.tw4_shift = it->second.shift;
+  ps.d.tw4_n = N;
+}
+
+// chirp c[l] = exp(-i*pi*(l^2 mod 2n)/n), l < n; filter = DFT_m(b)/m with
+// b[l] = conj(c[|l|]) on the wrapped indices (-n, n).
+void Builder::blue_for(int64_t n, int64_t m, PassSpec& ps) {
+  auto key = std::make_pair(n, m);
+  auto it = blue_cache.find(key);
+  if (it == blue_cache.end()) {
+    std::vector<cd> chirp(static_cast<size_t>(n)), b(size_t(m), cd(0, 0));
+    for (int64_t l = 0; l < n; ++l) {
+      const int64_t q = int64_t((__int128(l) * l) % (2 * n));
+      chirp[size_t(l)] = unit_root(q, 2 * n);  // exp(-2*pi*i*q/(2n)) = exp(-i*pi*q/n)
+    }
+    for (int64_t l = 0; l < n; ++l) {
+      b[size_t(l)] = std::conj(chirp[size_t(l)]);
+      if (l > 0) b[size_t(m - l)] = std::conj(chirp[size_t(l)]);
+    }
+    host_fft_fp64(b);
+    const double inv = 1.0 / double(m);
+    for (auto& v : b) v *= inv;
+    Blue bl;
+    bl.chirp = add(chirp);
+    bl.filter = add(b);
+    it = blue_cache.emplace(key, bl).first;
+  }
+  ps.chirp_off = int64_t(it->second.chirp);
+  ps.filter_off = int64_t(it->second.filter);
+}
+
+void choose_tile(PassSpec& ps, bool dbl) {
+  PassDesc& d = ps.d;
+  const int n = d.n;
+  const int eb = dbl ? 16 : 8;
+  int pitch = n + (n >> 4) + 1;
+  if (pitch % 2 == 0) ++pitch;
+  const int64_t smem_cap = 227 * 1024;
+  int wmax = int(smem_cap / (int64_t(2) * pitch * eb));
+  if (wmax < 1) wmax = 1;
+  const bool strided = (d.in_cs == 1 && d.in_es != 1) || (d.out_cs == 1 && d.out_es != 1);
+  const int target = dbl ? 2048 : 4096;
+  int W = std::max(1, target / n);
+  if (strided) W = std::max(W, 16);
+  W = std::min(W, wmax);
+  if (int64_t(W) > d.ncols) W = int(std::max<int64_t>(1, d.ncols));
+  d.W = W;
+  d.pitch = pitch;
+  d.threads = (int64_t(W) * n >= 8192) ? 512 : 256;
+  d.load_cfast = (d.in_cs == 1 && d.in_es != 1) ? 1 : 0;
+  d.store_cfast = (d.out_cs == 1 && d.out_es != 1) ? 1 : 0;
+}
+
+static PassSpec blank_pass() {
+  PassSpec ps;
+  std::memset(&ps.d, 0, sizeof(ps.d));
+  ps.d.nb_lo = 1;
+  ps.d.nbatch = 1;
+  ps.d.scale = 1.0;
+  ps.d.tw4_n = 1;
+  return ps;
+}
+
+// ---------------------------------------------------------------------------
+// Axis geometry: element (o, c, i) at o*os + c*cs + i*es, o < outer, c < ncols.
+struct Axis {
+  int64_t n, es, cs, ncols, os, outer;
+};
+
+static int cap_for(bool dbl) { return dbl ? kCapC64 : kCapC32; }
+
+// Split n = n1*n2 (n1 strided first pass, n2 second) with both <= cap,
+// n1 as close to sqrt(n) as possible.
+static bool split_four_step(int64_t n, int cap, int64_t& n1, int64_t& n2) {
+  int64_t best = 0;
+  double bestd = 1e300;
+  for (int64_t a = 2; a <= cap && a < n; ++a) {
+    if (n % a) continue;
+    const int64_t b = n / a;
+    if (b > cap || b < 2) continue;
+    const double dd = std::fabs(std::log(double(a)) - std::log(double(b)));
+    if (dd < bestd) {
+      bestd = dd;
+      best = a;
+    }
+  }
+  if (!best) return false;
+  n1 = best;
+  n2 = n / best;
+  return true;
+}
+
+// Appends the passes of one axis.  `first`: this axis reads the user's
+// input; later axes work on the output buffer.
+int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
+             int64_t& scratch1, int64_t& scratch2, std::string& desc) {
+  const bool dbl = B.dbl;
+  const int cap = cap_for(dbl);
+  const int src = first ? R_IN : R_OUT;
+  char buf[256];
+  if (ax.n <= 1) return GBFFT_OK;
+
+  if (is_fast_length(ax.n) && ax.n <= cap) {
+    PassSpec ps = blank_pass();
+    if (!B.stages_for(int(ax.n), ps)) return GBFFT_ERR_UNSUPPORTED;
+    PassDesc& d = ps.d;
+    d.in_es = d.out_es = ax.es;
+    d.in_cs = d.out_cs = ax.cs;
+    d.in_bs = d.out_bs = ax.os;
+    d.ncols = ax.ncols;
+    d.nbatch = d.nb_lo = ax.outer;
+    choose_tile(ps, dbl);
+    ps.src = src;
+    ps.dst = R_OUT;
+    passes.push_back(ps);
+    std::snprintf(buf, sizeof buf, "[n=%lld es=%lld W=%d]", (long long)ax.n, (long long)ax.es, ps.d.W);
+    desc += buf;
+    return GBFFT_OK;
+  }
+
+  if (is_fast_length(ax.n)) {
+    int64_t n1, n2;
+    if (!split_four_step(ax.n, cap, n1, n2)) return GBFFT_ERR_UNSUPPORTED;
+    PassSpec p1 = blank_pass(), p2 = blank_pass();
+    if (!B.stages_for(int(n1), p1) || !B.stages_for(int(n2), p2)) return GBFFT_ERR_UNSUPPORTED;
+    B.tw4_for(ax.n, p1);
+    p1.d.flags |= F_TW4;
+    const int mid = first ? R_OUT : R_S1;
+    if (!first) scratch1 = std::max(scratch1, ax.n * ax.ncols * ax.outer);
+    if (ax.es == 1) {
+      // contiguous rows: c indexes rows (stride cs)
+      PassDesc& a = p1.d;
+      a.nbatch = a.nb_lo = ax.ncols * ax.outer;
+      if (ax.outer > 1 && ax.os != ax.ncols * ax.cs) return GBFFT_ERR_UNSUPPORTED;
+      a.in_bs = a.out_bs = ax.cs;
+      a.ncols = n2;
+      a.in_cs = 1;
+      a.in_es = n2;
+      a.out_es = 1;
+      a.out_cs = n1;
+      PassDesc& b = p2.d;
+      b.nbatch = b.nb_lo = ax.ncols * ax.outer;
+      b.in_bs = b.out_bs = ax.cs;
+      b.ncols = n1;
+      b.in_cs = b.out_cs = 1;
+      b.in_es = b.out_es = n1;
+    } else {
+      // strided axis of stride S = es over cs == 1 columns
+      if (ax.cs != 1 || ax.ncols != ax.es) return GBFFT_ERR_UNSUPPORTED;
+      const int64_t S = ax.es;
+      PassDesc& a = p1.d;
+      a.nb_lo = n2;
+      a.nbatch = n2 * ax.outer;
+      a.in_bs = S;
+      a.out_bs = n1 * S;
+      a.in_bs2 = a.out_bs2 = ax.os;
+      a.ncols = S;
+      a.in_cs = a.out_cs = 1;
+      a.in_es = n2 * S;
+      a.out_es = S;
+      a.flags |= F_TW4_BATCH;
+      PassDesc& b = p2.d;
+      b.nb_lo = n1;
+      b.nbatch = n1 * ax.outer;
+      b.in_bs = b.out_bs = S;
+      b.in_bs2 = b.out_bs2 = ax.os;
+      b.ncols = S;
+      b.in_cs = b.out_cs = 1;
+      b.in_es = b.out_es = n1 * S;
+    }
+    choose_tile(p1, dbl);
+    choose_tile(p2, dbl);
+    p1.src = src;
+    p1.dst = mid;
+    p2.src = mid;
+    p2.dst = R_OUT;
+    passes.push_back(p1);
+    passes.push_back(p2);
+    std::snprintf(buf, sizeof buf, "[n=%lld=%lldx%lld four-step es=%lld W=%d,%d]", (long long)ax.n,
+                  (long long)n1, (long long)n2, (long long)ax.es, p1.d.W, p2.d.W);
+    desc += buf;
+    return GBFFT_OK;
+  }
+
+  // Bluestein
+  const int64_t m = bluestein_length(ax.n);
+  if (m <= cap) {
+    PassSpec ps = blank_pass();
+    if (!B.stages_for(int(m), ps)) return GBFFT_ERR_UNSUPPORTED;
+    B.blue_for(ax.n, m, ps);
+    PassDesc& d = ps.d;
+    d.in_es = d.out_es = ax.es;
+    d.in_cs = d.out_cs = ax.cs;
+    d.in_bs = d.out_bs = ax.os;
+    d.ncols = ax.ncols;
+    d.nbatch = d.nb_lo = ax.outer;
+    d.flags |= F_PAD_IN | F_CHIRP_IN | F_BLUE | F_TRUNC_OUT;
+    d.lin_es = 1;
+    d.lin_cs = 0;
+    d.lout_es = 1;
+    d.lout_cs = 0;
+    d.n_in = ax.n;
+    d.n_out = ax.n;
+    choose_tile(ps, dbl);
+    ps.src = src;
+    ps.dst = R_OUT;
+    passes.push_back(ps);
+    std::snprintf(buf, sizeof buf, "[n=%lld bluestein m=%lld es=%lld W=%d]", (long long)ax.n,
+                  (long long)m, (long long)ax.es, ps.d.W);
+    desc += buf;
+    return GBFFT_OK;
+  }
+
+  // multi-pass Bluestein: contiguous rows only
+  if (ax.es != 1) return GBFFT_ERR_UNSUPPORTED;
+  if (ax.outer > 1 && ax.os != ax.ncols * ax.cs) return GBFFT_ERR_UNSUPPORTED;
+  int64_t m1, m2;
+  if (!split_four_step(m, cap, m1, m2)) return GBFFT_ERR_UNSUPPORTED;
+  const int64_t rows = ax.ncols * ax.outer;
+  scratch1 = std::max(scratch1, rows * m);
+  scratch2 = std::max(scratch2, rows * m);
+  PassSpec p[4] = {blank_pass(), blank_pass(), blank_pass(), blank_pass()};
+  for (int i = 0; i < 4; ++i) {
+    if (!B.stages_for(int((i % 2 == 0) ? m1 : m2), p[i])) return GBFFT_ERR_UNSUPPORTED;
+    B.blue_for(ax.n, m, p[i]);
+    p[i].d.nbatch = p[i].d.nb_lo = rows;
+  }
+  // P1: src -> S1, chirp + zero pad, first four-step half, transposed store
+  {
+    PassDesc& d = p[0].d;
+    B.tw4_for(m, p[0]);
+    d.in_bs = ax.cs;
+    d.out_bs = m;
+    d.ncols = m2;
+    d.in_cs = 1;
+    d.in_es = m2;
+    d.out_es = 1;
+    d.out_cs = m1;
+    d.lin_es = m2;
+    d.lin_cs = 1;
+    d.n_in = ax.n;
+    d.flags |= F_PAD_IN | F_CHIRP_IN | F_TW4;
+  }
+  // P2: S1 in place, second half, filter multiply + conj
+  {
+    PassDesc& d = p[1].d;
+    d.in_bs = d.out_bs = m;
+    d.ncols = m1;
+    d.in_cs = d.out_cs = 1;
+    d.in_es = d.out_es = m1;
+    d.lout_es = m1;
+    d.lout_cs = 1;
+    d.flags |= F_FILTER_OUT;
+  }
+  // P3: S1 -> S2, first half of the inverse (as a forward transform)
+  {
+    PassDesc& d = p[2].d;
+    B.tw4_for(m, p[2]);
+    d.in_bs = d.out_bs = m;
+    d.ncols = m2;
+    d.in_cs = 1;
+    d.in_es = m2;
+    d.out_es = 1;
+    d.out_cs = m1;
+    d.flags |= F_TW4;
+  }
+  // P4: S2 -> dst, second half, conj + chirp, first n outputs
+  {
+    PassDesc& d = p[3].d;
+    d.in_bs = m;
+    d.out_bs = ax.cs;
+    d.ncols = m1;
+    d.in_cs = d.out_cs = 1;
+    d.in_es = d.out_es = m1;
+    d.lout_es = m1;
+    d.lout_cs = 1;
+    d.n_out = ax.n;
+    d.flags |= F_CHIRP_OUT | F_TRUNC_OUT;
+  }
+  p[0].src = src;
+  p[0].dst = R_S1;
+  p[1].src = R_S1;
+  p[1].dst = R_S1;
+  p[2].src = R_S1;
+  p[2].dst = R_S2;
+  p[3].src = R_S2;
+  p[3].dst = R_OUT;
+  for (int i = 0; i < 4; ++i) {
+    choose_tile(p[i], dbl);
+    passes.push_back(p[i]);
+  }
+  std::snprintf(buf, sizeof buf, "[n=%lld bluestein m=%lld=%lldx%lld 4-pass]", (long long)ax.n,
+                (long long)m, (long long)m1, (long long)m2);
+  desc += buf;
+  return GBFFT_OK;
+}
+
+bool fault_injected(const char* what) {
+  const char* e = std::getenv("GBFFT_FAULT_INJECT");
+  return e && std::strstr(e, what) != nullptr;
+}
+
+}  // namespace gbfft
+
+using namespace gbfft;
+
+namespace gbfft {
+
+int build_plan(gbfft_plan* p, bool dry) {
+  Builder B;
+  B.dbl = p->dbl;
+  const int64_t* dm = p->dims;
+  std::vector<Axis> axes;
+  const int r = p->rank;
+  const int64_t w = dm[r - 1];
+  const int64_t rows = p->total / std::max<int64_t>(1, w);
+  // innermost axis: contiguous rows
+  axes.push_back(Axis{w, 1, w, rows, rows * w, 1});
+  if (p->kind == GBFFT_KIND_FULL) {
+    if (r == 2) axes.push_back(Axis{dm[0], w, 1, w, dm[0] * w, 1});
+    if (r == 3) {
+      const int64_t d0 = dm[0], h = dm[1];
+      axes.push_back(Axis{h, w, 1, w, h * w, d0});   // y: stride w, outer z
+      axes.push_back(Axis{d0, h * w, 1, h * w, d0 * h * w, 1});  // z
+    }
+  }
+  // A four-step axis writes a transposed intermediate and must read the
+  // user's input to avoid scratch: put the first such axis first.
+  const int cap = cap_for(p->dbl);
+  std::stable_sort(axes.begin(), axes.end(), [&](const Axis& a, const Axis& b) {
+    const bool fa = is_fast_length(a.n) && a.n > cap;
+    const bool fb = is_fast_length(b.n) && b.n > cap;
+    return fa && !fb;
+  });
+  int64_t s1 = 0, s2 = 0;
+  char head[128];
+  std::snprintf(head, sizeof head, "%s %s rank%d", p->dbl ? "c64" : "c32",
+                p->kind == GBFFT_KIND_FULL ? "full" : "many", r);
+  p->desc = head;
+  bool first = true;
+  for (const Axis& ax : axes) {
+    if (ax.n <= 1) continue;
+    const size_t before = p->passes.size();
+    int st = add_axis(B, p->passes, ax, first, s1, s2, p->desc);
+    if (st != GBFFT_OK) return st;
+    if (p->passes.size() > before) first = false;
+  }
+  // device tables
+  const size_t eb = p->dbl ? 16 : 8;
+  if (dry) {
+    p->tables_bytes = B.blob.size();
+    p->scratch_bytes = size_t(s1 + s2) * eb;
+    return GBFFT_OK;
+  }
+  if (!B.blob.empty()) {
+    if (fault_injected("alloc")) return GBFFT_ERR_ALLOC;
+    p->tables_bytes = B.blob.size();
+    if (cudaMalloc(&p->d_tables, p->tables_bytes) != cudaSuccess) return GBFFT_ERR_ALLOC;
+    if (cudaMemcpy(p->d_tables, B.blob.data(), p->tables_bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+      return GBFFT_ERR_CUDA;
+  }
+  if (s1 + s2 > 0) {
+    if (fault_injected("alloc")) return GBFFT_ERR_ALLOC;
+    const size_t b1 = ((size_t(s1) * eb) + 255) & ~size_t(255);
+    p->s2_off = b1;
+    p->scratch_bytes = b1 + size_t(s2) * eb;
+    if (cudaMalloc(&p->d_scratch, p->scratch_bytes) != cudaSuccess) return GBFFT_ERR_ALLOC;
+  }
+  unsigned char* base = static_cast<unsigned char*>(p->d_tables);
+  for (PassSpec& ps : p->passes) {
+    if (ps.tw_off >= 0) ps.d.tw = base + ps.tw_off;
+    if (ps.tw4lo_off >= 0) ps.d.tw4_lo = base + ps.tw4lo_off;
+    if (ps.tw4hi_off >= 0) ps.d.tw4_hi = base + ps.tw4hi_off;
+    if (ps.chirp_off >= 0) ps.d.chirp = base + ps.chirp_off;
+    if (ps.filter_off >= 0) ps.d.filter = base + ps.filter_off;
+  }
+  if (std::getenv("GBFFT_PLAN_DUMP")) std::fprintf(stderr, "gbfft plan: %s\n", p->desc.c_str());
+  return GBFFT_OK;
+}
+
+void* role_ptr(const gbfft_plan* p, int role, const void* in, void* out) {
+  switch (role) {
+    case R_IN: return const_cast<void*>(in);
+    case R_OUT: return out;
+    case R_S1: return p->d_scratch;
+    case R_S2: return static_cast<unsigned char*>(p->d_scratch) + p->s2_off;
+  }
+  return nullptr;
+}
+
+int exec_passes(const gbfft_plan* p, const std::vector<PassSpec>& passes, int mode, double inv_norm,
+                const void* in, void* out, cudaStream_t s) {
+  if (passes.empty()) {
+    // every axis has length <= 1: the DFT is the identity
+    const size_t bytes = size_t(p->total) * (p->dbl ? 16 : 8);
+    if (bytes && cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+      return GBFFT_ERR_CUDA;
+    return GBFFT_OK;
+  }
+  const size_t last = passes.size() - 1;
+  for (size_t i = 0; i < passes.size(); ++i) {
+    PassDesc d = passes[i].d;
+    d.in = role_ptr(p, passes[i].src, in, out);
+    d.out = role_ptr(p, passes[i].dst, in, out);
+    if (mode != GBFFT_FORWARD) {
+      if (i == 0) d.flags |= F_CONJ_IN;
+      if (i == last) d.flags |= F_CONJ_OUT;
+    }
+    if (mode == GBFFT_INVERSE && i == last) {
+      d.flags |= F_SCALE;
+      d.scale = inv_norm;
+    }
+    if (launch_pass(d, p->dbl, s) != cudaSuccess) return GBFFT_ERR_CUDA;
+  }
+  return GBFFT_OK;
+}
+
+}  // namespace gbfft
+
+// ---------------------------------------------------------------------------
+// C ABI
+extern "C" {
+
+const char* gbfft_error_string(int status) {
+  switch (status) {
+    case GBFFT_OK: return "ok";
+    case GBFFT_ERR_INVALID_ARG: return "invalid argument";
+    case GBFFT_ERR_UNSUPPORTED: return "unsupported transform for this build";
+    case GBFFT_ERR_ALLOC: return "allocation failed";
+    case GBFFT_ERR_CUDA: return "CUDA runtime error";
+    case GBFFT_ERR_NULL_PLAN: return "null plan";
+    case GBFFT_ERR_TIMEOUT: return "bounded device wait timed out";
+    case GBFFT_ERR_INTERNAL: return "internal error";
+  }
+  return "unknown status";
+}
+
+int gbfft_version(void) { return 10000 * 0 + 100 * 1 + 0; }
+
+int gbfft_plan_create(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype,
+                      int precision) {
+  if (!out) return GBFFT_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (rank < 1 || rank > 3 || !dims) return GBFFT_ERR_INVALID_ARG;
+  if (kind != GBFFT_KIND_MANY && kind != GBFFT_KIND_FULL) return GBFFT_ERR_INVALID_ARG;
+  if (dtype != GBFFT_C32 && dtype != GBFFT_C64) return GBFFT_ERR_INVALID_ARG;
+  if (precision != GBFFT_PLAIN && precision != GBFFT_SPLIT_FP16) return GBFFT_ERR_INVALID_ARG;
+  int64_t total = 1;
+  for (int i = 0; i < rank; ++i) {
+    if (dims[i] < 0) return GBFFT_ERR_INVALID_ARG;
+    if (dims[i] > 0 && total > (int64_t(1) << 40) / dims[i]) return GBFFT_ERR_UNSUPPORTED;
+    total *= dims[i];
+  }
+  if (precision == GBFFT_SPLIT_FP16 && dtype != GBFFT_C32) return GBFFT_ERR_INVALID_ARG;
+  std::unique_ptr<gbfft_plan> p(new gbfft_plan);
+  p->rank = rank;
+  for (int i = 0; i < rank; ++i) p->dims[i] = dims[i];
+  p->kind = kind;
+  p->dtype = dtype;
+  p->precision = precision;
+  p->dbl = dtype == GBFFT_C64;
+  p->total = total;
+  if (cudaGetDevice(&p->device) != cudaSuccess) return GBFFT_ERR_CUDA;
+  if (prepare_kernels() != cudaSuccess) return GBFFT_ERR_CUDA;
+  const int64_t norm = (kind == GBFFT_KIND_FULL) ? total : dims[rank - 1];
+  p->inv_norm = norm > 0 ? 1.0 / double(norm) : 1.0;
+  if (total > 0) {
+    if (precision == GBFFT_SPLIT_FP16) {
+      int st = build_split_plan(p.get());
+      if (st != GBFFT_OK) {
+        gbfft_plan_destroy(p.release());
+        return st;
+      }
+    } else {
+      int st = build_plan(p.get(), false);
+      if (st != GBFFT_OK) {
+        gbfft_plan_destroy(p.release());
+        return st;
+      }
+    }
+  }
+  *out = p.release();
+  return GBFFT_OK;
+}
+
+int gbfft_plan_explain(int rank, const int64_t* dims, int kind, int dtype, int precision, char* buf,
+                       size_t cap) {
+  if (!buf || cap == 0 || !dims || rank < 1 || rank > 3) return GBFFT_ERR_INVALID_ARG;
+  if (kind != GBFFT_KIND_MANY && kind != GBFFT_KIND_FULL) return GBFFT_ERR_INVALID_ARG;
+  if (dtype != GBFFT_C32 && dtype != GBFFT_C64) return GBFFT_ERR_INVALID_ARG;
+  gbfft_plan p;
+  p.rank = rank;
+  p.total = 1;
+  for (int i = 0; i < rank; ++i) {
+    if (dims[i] < 0) return GBFFT_ERR_INVALID_ARG;
+    p.dims[i] = dims[i];
+    p.total *= dims[i];
+  }
+  p.kind = kind;
+  p.dtype = dtype;
+  p.precision = precision;
+  p.dbl = dtype == GBFFT_C64;
+  if (precision != GBFFT_PLAIN) return GBFFT_ERR_UNSUPPORTED;
+  int st = p.total > 0 ? build_plan(&p, true) : GBFFT_OK;
+  if (st != GBFFT_OK) return st;
+  std::snprintf(buf, cap, "%s; launches=%d tables=%zu scratch=%zu", p.desc.c_str(),
+                int(p.passes.size()), p.tables_bytes, p.scratch_bytes);
+  return GBFFT_OK;
+}
+
+int gbfft_plan_destroy(gbfft_plan* plan) {
+  if (!plan) return GBFFT_OK;
+  if (plan->d_tables) cudaFree(plan->d_tables);
+  if (plan->d_scratch) cudaFree(plan->d_scratch);
+  delete plan;
+  return GBFFT_OK;
+}
+
+int gbfft_exec(const gbfft_plan* plan, int mode, const void* d_in, void* d_out, void* stream) {
+  if (!plan) return GBFFT_ERR_NULL_PLAN;
+  if (mode != GBFFT_FORWARD && mode != GBFFT_REVERSE && mode != GBFFT_INVERSE)
+    return GBFFT_ERR_INVALID_ARG;
+  if (plan->total == 0) return GBFFT_OK;
+  if (!d_in || !d_out || d_in == d_out) return GBFFT_ERR_INVALID_ARG;
+  const uintptr_t align = plan->dbl ? 16 : 8;
+  if ((reinterpret_cast<uintptr_t>(d_in) | reinterpret_cast<uintptr_t>(d_out)) & (align - 1))
+    return GBFFT_ERR_INVALID_ARG;
+  return exec_passes(plan, plan->passes, mode, plan->inv_norm, d_in, d_out,
+                     static_cast<cudaStream_t>(stream));
+}
+
+// ---- plan cache -----------------------------------------------------------
+namespace {
+using CacheKey = std::tuple<uintptr_t, int, int64_t, int64_t, int64_t, int, int, int>;
+std::mutex g_cache_mu;
+std::map<CacheKey, gbfft_plan*>& cache() {
+  static auto* m = new std::map<CacheKey, gbfft_plan*>();
+  return *m;
+}
+
+uintptr_t current_context() {
+  static PFN_cuCtxGetCurrent_v4000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f);
+  }();
+  CUcontext c = nullptr;
+  if (fn) fn(&c);
+  if (!c) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return uintptr_t(0x1000 + dev);
+  }
+  return reinterpret_cast<uintptr_t>(c);
+}
+}  // namespace
+
+int gbfft_plan_get(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype,
+                   int precision) {
+  if (!out || !dims || rank < 1 || rank > 3) return GBFFT_ERR_INVALID_ARG;
+  // make sure a context exists before keying on it
+  cudaFree(nullptr);
+  int64_t d[3] = {0, 0, 0};
+  for (int i = 0; i < rank; ++i) d[i] = dims[i];
+  CacheKey key{current_context(), rank, d[0], d[1], d[2], kind, dtype, precision};
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  auto it = cache().find(key);
+  if (it != cache().end()) {
+    *out = it->second;
+    return GBFFT_OK;
+  }
+  gbfft_plan* p = nullptr;
+  int st = gbfft_plan_create(&p, rank, dims, kind, dtype, precision);
+  if (st != GBFFT_OK) return st;
+  cache().emplace(key, p);
+  *out = p;
+  return GBFFT_OK;
+}
+
+int gbfft_fft(int mode, int rank, const int64_t* dims, int kind, int dtype, const void* d_in,
+              void* d_out, void* stream) {
+  gbfft_plan* p = nullptr;
+  int st = gbfft_plan_get(&p, rank, dims, kind, dtype, GBFFT_PLAIN);
+  if (st != GBFFT_OK) return st;
+  return gbfft_exec(p, mode, d_in, d_out, stream);
+}
+
+int gbfft_cache_clear(void) {
+  const uintptr_t ctx = current_context();
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  for (auto it = cache().begin(); it != cache().end();) {
+    if (std::get<0>(it->first) == ctx) {
+      gbfft_plan_destroy(it->second);
+      it = cache().erase(it);
+    } else {
+      ++it;
+    }
+  }
+  return GBFFT_OK;
+}
+
+int gbfft_exec_range(const gbfft_plan* plan, int mode, int first, int count, const void* d_in,
+                     void* d_out, void* stream) {
+  if (!plan) return GBFFT_ERR_NULL_PLAN;
+  if (mode != GBFFT_FORWARD && mode != GBFFT_REVERSE && mode != GBFFT_INVERSE)
+    return GBFFT_ERR_INVALID_ARG;
+  const int np = int(plan->passes.size());
+  if (first < 0 || count < 0 || first + count > np) return GBFFT_ERR_INVALID_ARG;
+  if (plan->total == 0 || count == 0) return GBFFT_OK;
+  if (!d_in || !d_out || d_in == d_out) return GBFFT_ERR_INVALID_ARG;
+  const size_t last = plan->passes.size() - 1;
+  for (int i = first; i < first + count; ++i) {
+    const PassSpec& ps = plan->passes[size_t(i)];
+    PassDesc d = ps.d;
+    d.in = role_ptr(plan, ps.src, d_in, d_out);
+    d.out = role_ptr(plan, ps.dst, d_in, d_out);
+    if (mode != GBFFT_FORWARD) {
+      if (i == 0) d.flags |= F_CONJ_IN;
+      if (size_t(i) == last) d.flags |= F_CONJ_OUT;
+    }
+    if (mode == GBFFT_INVERSE && size_t(i) == last) {
+      d.flags |= F_SCALE;
+      d.scale = plan->inv_norm;
+    }
+    if (launch_pass(d, plan->dbl, static_cast<cudaStream_t>(stream)) != cudaSuccess)
+      return GBFFT_ERR_CUDA;
+  }
+  return GBFFT_OK;
+}
+
+int gbfft_plan_info(const gbfft_plan* plan, size_t* workspace_bytes, int* launches_per_exec) {
+  if (!plan) return GBFFT_ERR_NULL_PLAN;
+  if (workspace_bytes) *workspace_bytes = plan->tables_bytes + plan->scratch_bytes;
+  if (launches_per_exec) *launches_per_exec = int(plan->passes.size());
+  return GBFFT_OK;
+}
+
+int gbfft_plan_describe(const gbfft_plan* plan, char* buf, size_t cap) {
+  if (!plan) return GBFFT_ERR_NULL_PLAN;
+  if (!buf || cap == 0) return GBFFT_ERR_INVALID_ARG;
+  std::snprintf(buf, cap, "%s", plan->desc.c_str());
+  return GBFFT_OK;
+}
+
+}  // extern "C"

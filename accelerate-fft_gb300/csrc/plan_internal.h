@@ -1,0 +1,89 @@
+// Host-side planner internals shared by the plan, ragged, spectral-convolution
+// and split-precision translation units.
+#pragma once
+
+#include <complex>
+#include <cstdint>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "gbfft_internal.h"
+
+namespace gbfft {
+
+using cd = std::complex<double>;
+
+// Buffer roles of a pass: the user's input / output, or plan scratch.
+enum Role { R_IN = 0, R_OUT = 1, R_S1 = 2, R_S2 = 3 };
+
+struct PassSpec {
+  PassDesc d;
+  int src = R_IN, dst = R_OUT;
+  // byte offsets into the plan's table blob (-1: none)
+  int64_t tw_off = -1, tw4lo_off = -1, tw4hi_off = -1, chirp_off = -1, filter_off = -1;
+};
+
+// Accumulates the device tables of a plan (stage twiddles, four-step
+// twiddles, Bluestein chirps and filter spectra) in one host blob, with
+// per-length caches so repeated lengths share one copy.
+struct Builder {
+  bool dbl = false;
+  std::vector<unsigned char> blob;
+  struct StageTable {
+    size_t off = 0;
+    std::vector<int> offs;
+  };
+  struct Tw4 {
+    size_t lo = 0, hi = 0;
+    int shift = 0;
+  };
+  struct Blue {
+    size_t chirp = 0, filter = 0;
+  };
+  std::map<int64_t, StageTable> stage_cache;
+  std::map<int64_t, Tw4> tw4_cache;
+  std::map<std::pair<int64_t, int64_t>, Blue> blue_cache;
+
+  size_t add(const std::vector<cd>& v);
+  bool stages_for(int n, PassSpec& ps);
+  void tw4_for(int64_t N, PassSpec& ps);
+  void blue_for(int64_t n, int64_t m, PassSpec& ps);
+};
+
+cd unit_root(int64_t t, int64_t L);  // exp(-2*pi*i*t/L), exact reduction
+bool factor_device(int64_t n, std::vector<int>& out);
+bool is_fast_length(int64_t n);
+int64_t bluestein_length(int64_t n);
+void host_fft_fp64(std::vector<cd>& x);
+void choose_tile(PassSpec& ps, bool dbl);
+bool fault_injected(const char* what);
+
+}  // namespace gbfft
+
+// The plan object behind the opaque gbfft_plan handle.
+struct gbfft_plan {
+  int rank = 0;
+  int64_t dims[3] = {0, 0, 0};
+  int kind = 0, dtype = 0, precision = 0;
+  int device = 0;
+  bool dbl = false;
+  int64_t total = 0;
+  double inv_norm = 1.0;
+  std::vector<gbfft::PassSpec> passes;
+  void* d_tables = nullptr;
+  size_t tables_bytes = 0;
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  size_t s2_off = 0;
+  std::string desc;
+};
+
+
+namespace gbfft {
+int build_plan(gbfft_plan* p, bool dry);
+int build_split_plan(gbfft_plan* p);
+int exec_passes(const gbfft_plan* p, const std::vector<PassSpec>& passes, int mode, double inv_norm,
+                const void* in, void* out, cudaStream_t s);
+}  // namespace gbfft

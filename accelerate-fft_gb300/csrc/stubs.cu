@@ -1,0 +1,34 @@
+// Entry points of subsystems that are not built yet report
+// GBFFT_ERR_UNSUPPORTED so the C ABI stays complete.
+#include "gbfft.h"
+#include "plan_internal.h"
+
+namespace gbfft {
+int build_split_plan(gbfft_plan*) { return GBFFT_ERR_UNSUPPORTED; }
+}  // namespace gbfft
+
+extern "C" {
+int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t, const int64_t*, const int64_t*,
+                             const int*, int) {
+  if (out) *out = nullptr;
+  return GBFFT_ERR_UNSUPPORTED;
+}
+int gbfft_ragged_exec(const gbfft_ragged_plan*, const void*, void*, void*) { return GBFFT_ERR_UNSUPPORTED; }
+int gbfft_ragged_exec_per_transform(const gbfft_ragged_plan*, const void*, void*, void*) {
+  return GBFFT_ERR_UNSUPPORTED;
+}
+int gbfft_ragged_plan_destroy(gbfft_ragged_plan*) { return GBFFT_OK; }
+int gbfft_ragged_status(const gbfft_ragged_plan*, void*) { return GBFFT_ERR_UNSUPPORTED; }
+int gbfft_specconv_plan_create(gbfft_specconv_plan** out, int64_t, int64_t, int64_t, int64_t, int) {
+  if (out) *out = nullptr;
+  return GBFFT_ERR_UNSUPPORTED;
+}
+int gbfft_specconv_fwd(const gbfft_specconv_plan*, const void*, const void*, void*, void*) {
+  return GBFFT_ERR_UNSUPPORTED;
+}
+int gbfft_specconv_bwd(const gbfft_specconv_plan*, const void*, const void*, const void*, void*, void*,
+                       void*) {
+  return GBFFT_ERR_UNSUPPORTED;
+}
+int gbfft_specconv_plan_destroy(gbfft_specconv_plan*) { return GBFFT_OK; }
+}

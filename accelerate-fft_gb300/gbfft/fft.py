@@ -1,0 +1,152 @@
+"""The accelerate-fft API over the C ABI.
+
+``fft`` transforms the innermost axis of a rank >= 1 array (FFT.hs:63-84; the
+PTX path's "cuda.fft2.many" / "cuda.fft3.many", PTX.hs:52-61); ``fft1D``,
+``fft2D``, ``fft3D`` transform every axis (FFT.hs:92-173, PTX.hs:63-70).
+Inverse is normalised by the innermost length for ``fft`` and by the array
+size for the others, as in FFT.hs:69,98,125,155 -- but inside the kernel, so
+no extra elementwise pass runs.  Results are new tensors; inputs are never
+modified.
+"""
+import ctypes
+import enum
+
+import torch
+
+from . import _lib as L
+
+
+class Mode(enum.IntEnum):
+    """src/Data/Array/Accelerate/Math/FFT/Mode.hs:15-26."""
+    Forward = L.FORWARD
+    Reverse = L.REVERSE
+    Inverse = L.INVERSE
+
+
+def mode_code(mode):
+    if isinstance(mode, str):
+        return int(Mode[mode.capitalize()])
+    m = int(mode)
+    if m not in (L.FORWARD, L.REVERSE, L.INVERSE):
+        raise ValueError("mode must be Forward, Reverse or Inverse")
+    return m
+
+
+def _dtype_code(t):
+    if t.dtype == torch.complex64:
+        return L.C32
+    if t.dtype == torch.complex128:
+        return L.C64
+    raise TypeError("gbfft: complex64 or complex128 tensor required, got %s" % t.dtype)
+
+
+def _stream(stream):
+    if stream is None:
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, torch.cuda.Stream):
+        return ctypes.c_void_p(stream.cuda_stream)
+    return ctypes.c_void_p(int(stream))
+
+
+def _dims(shape):
+    return (ctypes.c_int64 * len(shape))(*[int(s) for s in shape])
+
+
+class Plan:
+    """An owned plan (gbfft_plan_create / gbfft_exec / gbfft_plan_destroy)."""
+
+    def __init__(self, shape, kind="full", dtype=torch.complex64, precision="plain"):
+        self.shape = tuple(int(s) for s in shape)
+        self.kind = L.KIND_FULL if kind == "full" else L.KIND_MANY
+        self.dtype = dtype
+        self.dtype_code = L.C64 if dtype == torch.complex128 else L.C32
+        self.precision = L.SPLIT_FP16 if precision == "split_fp16" else L.PLAIN
+        h = ctypes.c_void_p()
+        L.check(L.lib().gbfft_plan_create(ctypes.byref(h), len(self.shape), _dims(self.shape),
+                                          self.kind, self.dtype_code, self.precision),
+                "gbfft_plan_create%s" % (self.shape,))
+        self.handle = h
+
+    def exec_ptr(self, mode, in_ptr, out_ptr, stream=None):
+        L.check(L.lib().gbfft_exec(self.handle, mode_code(mode), ctypes.c_void_p(in_ptr),
+                                   ctypes.c_void_p(out_ptr), _stream(stream)), "gbfft_exec")
+
+    def __call__(self, mode, x, out=None, stream=None):
+        if not x.is_cuda or not x.is_contiguous():
+            raise ValueError("gbfft: contiguous CUDA tensor required")
+        if tuple(x.shape) != self.shape or x.dtype != self.dtype:
+            raise ValueError("gbfft: tensor does not match the plan")
+        if out is None:
+            out = torch.empty_like(x)
+        self.exec_ptr(mode, x.data_ptr(), out.data_ptr(), stream)
+        return out
+
+    @property
+    def info(self):
+        ws = ctypes.c_size_t()
+        n = ctypes.c_int()
+        L.check(L.lib().gbfft_plan_info(self.handle, ctypes.byref(ws), ctypes.byref(n)))
+        return {"workspace_bytes": ws.value, "launches": n.value}
+
+    def describe(self):
+        buf = ctypes.create_string_buffer(4096)
+        L.check(L.lib().gbfft_plan_describe(self.handle, buf, 4096))
+        return buf.value.decode()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            L.lib().gbfft_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _run(kind, mode, arr, stream=None):
+    if not isinstance(arr, torch.Tensor) or not arr.is_cuda:
+        raise TypeError("gbfft: a CUDA tensor is required")
+    dt = _dtype_code(arr)
+    x = arr.contiguous()
+    out = torch.empty_like(x)
+    shape = tuple(x.shape)
+    if x.numel() == 0:
+        return out
+    L.check(L.lib().gbfft_fft(mode_code(mode), len(shape), _dims(shape), kind, dt,
+                              ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                              _stream(stream)), "gbfft_fft%s" % (shape,))
+    return out
+
+
+def fft(mode, arr, stream=None):
+    """DFT along the innermost axis (FFT.hs:63-84); any rank >= 1."""
+    if arr.dim() < 1:
+        raise ValueError("fft: rank >= 1 required")
+    if arr.dim() > 3:
+        # rank 4+: the batched-innermost plan over the flattened outer axes
+        flat = arr.contiguous().reshape(-1, arr.shape[-1])
+        return _run(L.KIND_MANY, mode, flat, stream).reshape(arr.shape)
+    return _run(L.KIND_MANY, mode, arr, stream)
+
+
+def fft1D(mode, arr, stream=None):
+    """DFT of a vector (FFT.hs:92-111)."""
+    if arr.dim() != 1:
+        raise ValueError("fft1D: rank 1 required")
+    return _run(L.KIND_FULL, mode, arr, stream)
+
+
+def fft2D(mode, arr, stream=None):
+    """DFT of a matrix (FFT.hs:119-142)."""
+    if arr.dim() != 2:
+        raise ValueError("fft2D: rank 2 required")
+    return _run(L.KIND_FULL, mode, arr, stream)
+
+
+def fft3D(mode, arr, stream=None):
+    """DFT of a 3D array (FFT.hs:150-173)."""
+    if arr.dim() != 3:
+        raise ValueError("fft3D: rank 3 required")
+    return _run(L.KIND_FULL, mode, arr, stream)

@@ -1,0 +1,383 @@
+"""Benchmark of the accelerate-fft GPU path on GB300.
+
+Default workload: fft2D Forward on a 4096 x 4096 Complex Float array,
+components i.i.d. N(0, 1) from a seed (the reference's headline
+configuration: PTX.fft2D, PTX.hs:66-67).  Metric: FFT GFLOP/s with the
+algorithmic count 5 N log2 N (N = 4096^2), plus the HBM roofline fraction of
+the dominant kernel and of the whole transform.
+
+One JSON line on rank 0.  `--impl reference` times the reference's CPU
+implementation of the same path (the oracle's restatement of the pure
+Accelerate transform, oracle/adhoc.cpp) on the host cores instead.
+
+Timing: W warm-up steps, then K timed steps; each step is timed with CUDA
+events on the launching stream and L2 is flushed (a 256 MiB write) between
+steps, outside the events.  The working set (2 x 128 MiB) also exceeds L2.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "accelerate-fft_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = ("FFT GFLOP/s (5N·log2N/t) + % HBM roofline: split-FP16 vs FP32 at "
+          "≤2e-6 rel err")
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# ---------------------------------------------------------------------------
+# workloads
+WORKLOADS = {
+    "fft2d_4096": dict(kind="full", shape=(4096, 4096), dtype="c32", mode="forward",
+                       desc="fft2D Forward, Complex Float 4096x4096, N(0,1)"),
+    "many_65536x1000": dict(kind="many", shape=(65536, 1000), dtype="c32", mode="forward",
+                            desc="fft innermost, Complex Float 65536x1000 (8*5*5*5), N(0,1)"),
+    "many_4096x1009": dict(kind="many", shape=(4096, 1009), dtype="c32", mode="forward",
+                           desc="fft innermost, Complex Float 4096x1009 (Bluestein), N(0,1)"),
+    "fft1d_1024_c64": dict(kind="full", shape=(1024,), dtype="c64", mode="forward",
+                           desc="fft1D Forward, Complex Double N=1024, U[-1,1]"),
+}
+
+
+def flops_of(shape, kind):
+    if kind == "full":
+        n = math.prod(shape)
+        return 5.0 * n * math.log2(n)
+    rows = math.prod(shape[:-1])
+    n = shape[-1]
+    return 5.0 * rows * n * math.log2(n) if n > 1 else 0.0
+
+
+def make_input(shape, dtype, seed):
+    import torch
+    g = torch.Generator().manual_seed(seed)
+    real_t = torch.float64 if dtype == "c64" else torch.float32
+    re = torch.randn(shape, generator=g, dtype=real_t)
+    im = torch.randn(shape, generator=g, dtype=real_t)
+    return torch.complex(re, im)
+
+
+def cpu_oracle_run(wl, x_np, threads):
+    from oracle import lib as O
+    fn = {"full": {1: O.fft1D, 2: O.fft2D, 3: O.fft3D}[len(wl["shape"])], "many": O.fft}[wl["kind"]]
+    return fn(0 if wl["mode"] == "forward" else 2, x_np, threads=threads)
+
+
+def cpu_baseline(wl, x_np, budget_s=12.0):
+    """The oracle timed on the host cores on a bounded sample of the workload."""
+    threads = os.cpu_count() or 1
+    shape = wl["shape"]
+    sample = x_np
+    rows_used = shape[0]
+    if wl["kind"] == "many":
+        # a bounded number of rows of the same length
+        rows_used = min(shape[0], 4096)
+        sample = x_np[:rows_used]
+    t0 = time.perf_counter()
+    cpu_oracle_run(wl, sample, threads)
+    one = time.perf_counter() - t0
+    reps = max(1, min(20, int(budget_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        cpu_oracle_run(wl, sample, threads)
+    dt = (time.perf_counter() - t0) / reps
+    sub_shape = (rows_used,) + tuple(shape[1:]) if wl["kind"] == "many" else shape
+    fl = flops_of(sub_shape, wl["kind"])
+    return {"value": fl / dt / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+            "sample": "%d run(s) of %s on shape %s (oracle C++ restatement of Adhoc.hs, OpenMP)"
+                      % (reps, wl["desc"], "x".join(map(str, sub_shape))),
+            "seconds_per_run": dt}
+
+
+def run_reference(args, wl):
+    world, rank, _ = dist_init()
+    if rank != 0:
+        return
+    import numpy as np
+    x = make_input(wl["shape"], wl["dtype"], 1234).numpy()
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_oracle_run(wl, x, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_oracle_run(wl, x, threads)
+    dt = (time.perf_counter() - t0) / args.steps
+    fl = flops_of(wl["shape"], wl["kind"])
+    val = fl / dt / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "GFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if wl["dtype"] == "c64" else "f32", "data": "synthetic",
+        "config": {"workload": wl["desc"], "shape": list(wl["shape"]), "seed": 1234},
+        "cpu_baseline": {"value": val, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                         "sample": "each step one full %s on the host cores (oracle C++ "
+                                   "restatement of the reference's pure-Accelerate transform; "
+                                   "the Haskell reference cannot be built offline)" % wl["desc"]},
+        "e2e": {"value": val, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gbfft(args, wl):
+    import numpy as np
+    import torch
+
+    import gbfft
+    from gbfft import _lib as L
+
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    lib = L.lib()
+    shape = wl["shape"]
+    dtype = torch.complex128 if wl["dtype"] == "c64" else torch.complex64
+    elem = 16 if wl["dtype"] == "c64" else 8
+    nelem = math.prod(shape)
+    x_cpu = make_input(shape, wl["dtype"], 1234 + rank)
+    x = x_cpu.to(dev)
+    y = torch.empty_like(x)
+    plan = gbfft.Plan(shape, kind=wl["kind"], dtype=dtype, precision=args.precision)
+    info = plan.info
+    npass = info["launches"]
+    mode = gbfft.mode_code(wl["mode"])
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def one_step(events=None):
+        if events is None:
+            L.check(lib.gbfft_exec(plan.handle, mode, ctypes.c_void_p(x.data_ptr()),
+                                   ctypes.c_void_p(y.data_ptr()), sp))
+            return
+        events[0].record(stream)
+        for i in range(npass):
+            L.check(lib.gbfft_exec_range(plan.handle, mode, i, 1, ctypes.c_void_p(x.data_ptr()),
+                                         ctypes.c_void_p(y.data_ptr()), sp))
+            events[i + 1].record(stream)
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(npass + 1)] for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        one_step(evs[k])
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop() if sampler else None
+    step_ms = [e[0].elapsed_time(e[-1]) for e in evs]
+    pass_ms = [[e[i].elapsed_time(e[i + 1]) for e in evs] for i in range(npass)]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms = total_ms / args.steps
+    fl = flops_of(shape, wl["kind"])
+    value = fl * world / (ms * 1e-3) / 1e9
+
+    peak, peak_kind = load_peaks()
+    bytes_pass = 2.0 * nelem * elem  # one compulsory read + write of the array per pass
+    avg_pass = [sum(p) / len(p) for p in pass_ms]
+    dom = max(range(npass), key=lambda i: avg_pass[i]) if npass else 0
+    ach = bytes_pass / (avg_pass[dom] * 1e-3) / 1e9 if npass else 0.0
+    ach_tr = bytes_pass / (ms * 1e-3) / 1e9
+
+    # accuracy of one result vs FP64 (numpy pocketfft), outside the timed region
+    rel_err = None
+    if rank == 0 and not args.no_check:
+        one_step()
+        torch.cuda.synchronize()
+        yy = y.cpu().numpy().astype(np.complex128)
+        xx = x_cpu.numpy().astype(np.complex128)
+        axes = tuple(range(len(shape))) if wl["kind"] == "full" else (-1,)
+        ref = np.fft.fftn(xx, axes=axes) if wl["mode"] == "forward" else np.fft.ifftn(xx, axes=axes)
+        rel_err = float(np.linalg.norm(yy - ref) / np.linalg.norm(ref))
+
+    # end to end through the C ABI with host buffers (pinned), H2D + exec + D2H
+    hx = x_cpu.pin_memory()
+    hy = torch.empty_like(hx).pin_memory()
+    e2e_ms = []
+    for k in range(max(3, min(args.steps, 20)) + 2):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        x.copy_(hx, non_blocking=True)
+        L.check(lib.gbfft_exec(plan.handle, mode, ctypes.c_void_p(x.data_ptr()),
+                               ctypes.c_void_p(y.data_ptr()), sp))
+        hy.copy_(y, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if k >= 2:
+            e2e_ms.append(e0.elapsed_time(e1))
+    e2e = fl * world / (statistics.mean(e2e_ms) * 1e-3) / 1e9
+
+    # cuFFT on the same input and timing (comparator only, not the product)
+    cufft_ms = None
+    if rank == 0 and not args.no_cufft:
+        f = (lambda t: torch.fft.fftn(t)) if wl["kind"] == "full" else (lambda t: torch.fft.fft(t, dim=-1))
+        for _ in range(3):
+            f(x)
+        ts = []
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            f(x)
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        cufft_ms = statistics.mean(ts)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(wl, x_cpu.numpy())
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if wl["dtype"] == "c64" else "f32", "data": "synthetic",
+            "config": {"workload": wl["desc"], "shape": list(shape), "kind": wl["kind"],
+                       "precision": args.precision, "seed": 1234,
+                       "l2": "flushed (256 MiB write) between timed steps; working set 2x%d MiB"
+                             % (nelem * elem >> 20),
+                       "plan": plan.describe(), "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                         "frac": ach / peak, "traffic": None, "peak_source": peak_kind,
+                         "kernel": "pass %d of %d (%s)" % (dom, npass, "pencil_kernel<float>"
+                                                           if elem == 8 else "pencil_kernel<double>"),
+                         "bytes_alg_per_launch": bytes_pass,
+                         "kernel_ms": avg_pass[dom] if npass else None},
+            "roofline_transform": {"achieved": ach_tr, "frac": ach_tr / peak,
+                                   "bytes_alg": bytes_pass, "pass_ms": avg_pass},
+            "rel_err_vs_fp64": rel_err,
+            "e2e": {"value": e2e, "unit": "GFLOP/s", "h2d_bytes_per_step": nelem * elem,
+                    "d2h_bytes_per_step": nelem * elem, "ms_per_step": statistics.mean(e2e_ms)},
+            "gpu_launches": args.steps * npass,
+            "clocks": clocks,
+            "cufft_comparator_ms": cufft_ms,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gbfft", choices=["gbfft", "reference"])
+    ap.add_argument("--workload", default="fft2d_4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="plain", choices=["plain", "split_fp16"])
+    ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--no-cufft", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_gbfft(args, wl)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,68 @@
+"""CPU tests of the C ABI boundary: libgbfft.so builds, loads, exports every
+function include/gbfft.h declares, and its host-only planner picks the
+expected passes (no GPU call)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "gbfft.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbfft_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(gbfft_lib):
+    from gbfft import _lib as L
+    lib = L.lib()
+    names = header_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in L.SIGNATURES, "python binding lacks " + n
+
+
+def test_error_strings_and_version(gbfft_lib):
+    from gbfft import _lib as L
+    lib = L.lib()
+    assert lib.gbfft_version() >= 100
+    for st in range(8):
+        assert lib.gbfft_error_string(st)
+    assert lib.gbfft_error_string(99) == b"unknown status"
+
+
+def explain(dims, kind=1, dtype=0, precision=0):
+    from gbfft import _lib as L
+    buf = ctypes.create_string_buffer(8192)
+    d = (ctypes.c_int64 * len(dims))(*dims)
+    st = L.lib().gbfft_plan_explain(len(dims), d, kind, dtype, precision, buf, 8192)
+    return st, buf.value.decode()
+
+
+def test_planner_choices(gbfft_lib):
+    st, s = explain((4096, 4096))
+    assert st == 0 and "launches=2" in s and "scratch=0" in s
+    st, s = explain((65536, 1000), kind=0)
+    assert st == 0 and "[n=1000 es=1" in s and "launches=1" in s
+    st, s = explain((4096, 1009), kind=0)
+    assert st == 0 and "bluestein m=2048" in s and "launches=1" in s
+    st, s = explain((65536,))
+    assert st == 0 and "four-step" in s and "launches=2" in s and "scratch=0" in s
+    st, s = explain((65521,))
+    assert st == 0 and "bluestein m=131072" in s and "4-pass" in s
+    st, s = explain((8192,), dtype=1)  # Complex Double: four-step above 4096
+    assert st == 0 and "four-step" in s
+    st, s = explain((256, 256, 256))
+    assert st == 0 and "launches=3" in s
+    st, s = explain((1, 1, 1))
+    assert st == 0 and "launches=0" in s
+
+
+def test_planner_rejects_bad_arguments(gbfft_lib):
+    assert explain((4, -1))[0] == 1
+    assert explain((4, 4), kind=9)[0] == 1
+    assert explain((4, 4), dtype=5)[0] == 1

@@ -1,0 +1,285 @@
+"""GPU parity: libgbfft (through its C ABI) against the oracle.
+
+Every result is compared (a) with an FP64 FFT of the same input (numpy's
+pocketfft; the oracle's FP64 restatement for the golden cases) and (b) with
+the oracle's restatement of the reference's own transform in the same
+precision (oracle/adhoc.cpp: Adhoc.hs + FFT.hs).
+
+Tolerances (relative L2):
+  complex64 vs FP64:  2e-6 (radix 2/3/4/5/7/8/16 stages, four-step), 4e-6
+                      (Bluestein, whose filter and chirp add two roundings)
+  complex128 vs FP64: 1e-12
+  vs the same-precision restatement: within the restatement's own FP64 error
+  plus the tolerance above (the reference's Float Bluestein forms its chirp
+  angle in single precision, Adhoc.hs:264-265, so it is itself ~1e-4 off).
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import lib as O
+from util import dim1, dim2, dim3, np_reference, rel_l2, uniform_complex
+
+pytestmark = pytest.mark.gpu
+
+MODES = ("forward", "reverse", "inverse")
+MODE_IDX = {"forward": 0, "reverse": 1, "inverse": 2}
+
+
+def fast(n):
+    for p in (2, 3, 5, 7):
+        while n % p == 0:
+            n //= p
+    return n == 1
+
+
+def tol_fp64(dtype, shape):
+    if dtype == np.complex128:
+        return 1e-12
+    return 2e-6 if all(fast(s) for s in shape) else 4e-6
+
+
+def run_gpu(g, kind, mode, x):
+    t = torch.from_numpy(x).cuda()
+    f = {"fft": g.fft, "fft1D": g.fft1D, "fft2D": g.fft2D, "fft3D": g.fft3D}[kind]
+    y = f(mode, t)
+    torch.cuda.synchronize()
+    assert torch.equal(t.cpu(), torch.from_numpy(x)), "input must be preserved"
+    return y.cpu().numpy()
+
+
+def check(g, kind, mode, x, same_precision=True):
+    y = run_gpu(g, kind, mode, x)
+    ref64 = np_reference(kind, MODE_IDX[mode], x)
+    e64 = rel_l2(y, ref64)
+    tol = tol_fp64(x.dtype.type, x.shape if kind != "fft" else x.shape[-1:])
+    assert e64 < tol, (kind, mode, x.shape, x.dtype, e64)
+    if same_precision:
+        r = O.run(kind, MODE_IDX[mode], x)
+        e_or = rel_l2(r, ref64)
+        assert rel_l2(y, r) <= 1.5 * e_or + 2 * tol, (kind, mode, x.shape, rel_l2(y, r), e_or)
+    return e64
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_fft1d_small_lengths_all_modes(gbfft_lib, dtype):
+    rng = np.random.default_rng(10)
+    for n in range(1, 130):
+        x = uniform_complex(rng, (n,), dtype)
+        for mode in MODES:
+            check(gbfft_lib, "fft1D", mode, x)
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_fft1d_reference_generator_lengths(gbfft_lib, dtype):
+    rng = np.random.default_rng(11)
+    for _ in range(40):
+        (n,) = dim1(rng)
+        x = uniform_complex(rng, (n,), dtype)
+        check(gbfft_lib, "fft1D", MODES[int(rng.integers(0, 3))], x)
+
+
+@pytest.mark.parametrize("n", [1000, 1009, 1024, 2048, 2025, 4096, 4097, 8192, 16384, 65536,
+                               65521, 5003, 100000, 3 * 5 * 7 * 11 * 13])
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_fft1d_paths(gbfft_lib, n, dtype):
+    # covers single-CTA radix, four-step (n > CTA capacity), single-kernel and
+    # four-pass Bluestein (prime n, padded length above the CTA capacity)
+    rng = np.random.default_rng(n)
+    x = uniform_complex(rng, (n,), dtype)
+    for mode in MODES:
+        check(gbfft_lib, "fft1D", mode, x, same_precision=(n <= 16384))
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_many_innermost_generator_shapes(gbfft_lib, dtype):
+    rng = np.random.default_rng(12)
+    for _ in range(12):
+        for gen in (dim2, dim3):
+            x = uniform_complex(rng, gen(rng), dtype)
+            check(gbfft_lib, "fft", MODES[int(rng.integers(0, 3))], x)
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_fft2d_fft3d_generator_shapes(gbfft_lib, dtype):
+    rng = np.random.default_rng(13)
+    for _ in range(12):
+        x = uniform_complex(rng, dim2(rng), dtype)
+        check(gbfft_lib, "fft2D", MODES[int(rng.integers(0, 3))], x)
+        x = uniform_complex(rng, dim3(rng), dtype)
+        check(gbfft_lib, "fft3D", MODES[int(rng.integers(0, 3))], x)
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (1, 7), (7, 1), (3, 8192), (8192, 3), (2, 16384),
+                                   (16384, 2), (600, 1009), (1009, 24), (12, 10007)])
+def test_fft2d_edge_shapes(gbfft_lib, shape):
+    rng = np.random.default_rng(sum(shape))
+    x = uniform_complex(rng, shape, np.complex64)
+    for mode in MODES:
+        check(gbfft_lib, "fft2D", mode, x, same_precision=max(shape) <= 8192)
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1), (2, 3, 5), (16, 32, 64), (64, 1, 1), (1, 1, 300),
+                                   (5, 9000, 2), (9000, 2, 3), (7, 11, 13)])
+def test_fft3d_edge_shapes(gbfft_lib, shape):
+    rng = np.random.default_rng(sum(shape))
+    x = uniform_complex(rng, shape, np.complex64)
+    for mode in MODES:
+        check(gbfft_lib, "fft3D", mode, x, same_precision=max(shape) <= 8192)
+
+
+def test_config1_fft1d_c64_roundtrip(gbfft_lib):
+    # fft1D Forward then Inverse on one Complex Double vector, N = 1024, U[-1, 1]
+    g = gbfft_lib
+    rng = np.random.default_rng(1024)
+    x = uniform_complex(rng, (1024,), np.complex128)
+    t = torch.from_numpy(x).cuda()
+    X = g.fft1D("forward", t)
+    xr = g.fft1D("inverse", X).cpu().numpy()
+    naive = O.dft_naive(-1, x)
+    assert rel_l2(X.cpu().numpy(), naive) < 1e-13
+    assert rel_l2(X.cpu().numpy(), O.fft1D(0, x)) < 1e-13
+    assert rel_l2(xr, x) < 1e-14
+
+
+# ---- reference properties (test/Test/FFT.hs:112-236) on the GPU -------------
+def _rev(x):
+    n = x.shape[-1]
+    return x[..., (-np.arange(n)) % n]
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+@pytest.mark.parametrize("gen,full", [(dim1, "fft1D"), (dim2, "fft2D"), (dim3, "fft3D")])
+def test_reference_properties_gpu(gbfft_lib, dtype, gen, full):
+    g = gbfft_lib
+    rng = np.random.default_rng(hash((full, str(dtype))) % 2**32)
+    tol = 1e-12 if dtype == np.complex128 else 1e-5
+    F = lambda m, a: run_gpu(g, full, m, a)
+    G = lambda m, a: run_gpu(g, "fft" if full != "fft1D" else "fft1D", m, a)
+    for _ in range(6):
+        sh = gen(rng)
+        mode = MODES[int(rng.integers(0, 3))]
+        x = uniform_complex(rng, sh, dtype)
+        y = uniform_complex(rng, sh, dtype)
+        a = uniform_complex(rng, (), dtype)
+        assert rel_l2(F(mode, (a * x).astype(dtype)), a * F(mode, x)) < tol           # homogeneity
+        assert rel_l2(F(mode, (x + y).astype(dtype)), F(mode, x) + F(mode, y)) < tol   # additivity
+        assert rel_l2(F("inverse", F("forward", x)), x) < tol                           # inverse
+        assert rel_l2(_rev(G(mode, x)), G(mode, _rev(x).copy())) < tol                  # reverse
+        assert rel_l2(np.conj(G(mode, x)), G(mode, np.conj(_rev(x)).astype(dtype))) < tol  # conjugate
+        m2 = MODES[int(rng.integers(0, 2))]
+        n = sh[-1]
+        fx, fy = G(m2, x).astype(np.complex128), G(m2, y).astype(np.complex128)
+        x64, y64 = x.astype(np.complex128), y.astype(np.complex128)
+        assert rel_l2(np.linalg.norm(fx, axis=-1), np.sqrt(n) * np.linalg.norm(x64, axis=-1)) < tol  # isometry
+        assert rel_l2(np.sum(fx * np.conj(fy), axis=-1), n * np.sum(x64 * np.conj(y64), axis=-1)) < 10 * tol  # unitarity
+
+
+# ---- full-size configurations through size-independent properties ---------
+def test_config2_fft2d_4096_full(gbfft_lib):
+    g = gbfft_lib
+    rng = np.random.default_rng(2)
+    x = (rng.standard_normal((4096, 4096)) + 1j * rng.standard_normal((4096, 4096))).astype(np.complex64)
+    t = torch.from_numpy(x).cuda()
+    y = g.fft2D("forward", t)
+    ref = np.fft.fft2(x.astype(np.complex128))
+    assert rel_l2(y.cpu().numpy(), ref) < 2e-6
+    back = g.fft2D("inverse", y)
+    assert rel_l2(back.cpu().numpy(), x) < 2e-6
+    # linearity at full size
+    s = g.fft2D("forward", 2.5 * t) - 2.5 * y
+    assert float(s.abs().max()) < 1e-3 * float(y.abs().max())
+
+
+def test_config3_many_full_sizes(gbfft_lib):
+    g = gbfft_lib
+    rng = np.random.default_rng(3)
+    for rows, n in ((65536, 1000), (4096, 1009)):
+        x = torch.complex(torch.randn(rows, n, generator=torch.Generator().manual_seed(n)),
+                          torch.randn(rows, n, generator=torch.Generator().manual_seed(n + 1)))
+        t = x.cuda()
+        y = g.fft("forward", t)
+        idx = rng.choice(rows, 64, replace=False)
+        sub = x.numpy()[idx].astype(np.complex128)
+        assert rel_l2(y.cpu().numpy()[idx], O.dft_naive(-1, sub)) < 4e-6
+        back = g.fft("inverse", y)
+        assert rel_l2(back.cpu().numpy(), x.numpy()) < 4e-6
+        # Parseval per row
+        ny = torch.linalg.vector_norm(y, dim=-1).double()
+        nx = torch.linalg.vector_norm(t, dim=-1).double() * np.sqrt(n)
+        assert float(((ny - nx).abs() / nx).max()) < 1e-5
+
+
+def test_config5_shape_3d_roundtrip(gbfft_lib):
+    g = gbfft_lib
+    t = torch.complex(torch.randn(256, 256, 256), torch.randn(256, 256, 256)).cuda()
+    y = g.fft3D("forward", t)
+    ref = torch.fft.fftn(t.to(torch.complex128))
+    err = float(torch.linalg.vector_norm(y.to(torch.complex128) - ref) / torch.linalg.vector_norm(ref))
+    assert err < 2e-6
+    back = g.fft3D("inverse", y)
+    assert float(torch.linalg.vector_norm(back - t) / torch.linalg.vector_norm(t)) < 2e-6
+
+
+# ---- edge cases and error behaviour -----------------------------------------
+def test_empty_and_unit_arrays(gbfft_lib):
+    g = gbfft_lib
+    for shape in ((0,), (0, 5), (5, 0), (3, 0, 2)):
+        t = torch.zeros(shape, dtype=torch.complex64, device="cuda")
+        assert g.fft("forward", t).shape == t.shape
+    t = torch.tensor([1.5 - 2j], dtype=torch.complex64, device="cuda")
+    for mode in MODES:
+        assert torch.equal(g.fft1D(mode, t), t)
+
+
+def test_error_codes(gbfft_lib):
+    import ctypes
+    from gbfft import _lib as L
+    lib = L.lib()
+    h = ctypes.c_void_p()
+    dims = (ctypes.c_int64 * 2)(4, 4)
+    assert lib.gbfft_plan_create(ctypes.byref(h), 0, dims, 1, 0, 0) == L.ERR_INVALID_ARG
+    assert lib.gbfft_plan_create(ctypes.byref(h), 4, dims, 1, 0, 0) == L.ERR_INVALID_ARG
+    assert lib.gbfft_plan_create(ctypes.byref(h), 2, dims, 7, 0, 0) == L.ERR_INVALID_ARG
+    assert lib.gbfft_plan_create(ctypes.byref(h), 2, dims, 1, 3, 0) == L.ERR_INVALID_ARG
+    neg = (ctypes.c_int64 * 2)(4, -1)
+    assert lib.gbfft_plan_create(ctypes.byref(h), 2, neg, 1, 0, 0) == L.ERR_INVALID_ARG
+    assert lib.gbfft_exec(None, -1, None, None, None) == L.ERR_NULL_PLAN
+    assert lib.gbfft_plan_create(ctypes.byref(h), 2, dims, 1, 0, 0) == L.OK
+    a = torch.zeros(16, dtype=torch.complex64, device="cuda")
+    b = torch.zeros(16, dtype=torch.complex64, device="cuda")
+    assert lib.gbfft_exec(h, 5, a.data_ptr(), b.data_ptr(), None) == L.ERR_INVALID_ARG
+    assert lib.gbfft_exec(h, -1, a.data_ptr(), a.data_ptr(), None) == L.ERR_INVALID_ARG
+    assert lib.gbfft_exec(h, -1, None, b.data_ptr(), None) == L.ERR_INVALID_ARG
+    assert lib.gbfft_exec(h, -1, a.data_ptr() + 4, b.data_ptr(), None) == L.ERR_INVALID_ARG
+    assert lib.gbfft_exec(h, -1, a.data_ptr(), b.data_ptr(), None) == L.OK
+    assert lib.gbfft_plan_destroy(h) == L.OK
+    with pytest.raises(TypeError):
+        g = gbfft_lib
+        g.fft("forward", torch.zeros(4, device="cuda"))
+
+
+def test_plan_cache_and_concurrent_streams(gbfft_lib):
+    g = gbfft_lib
+    rng = np.random.default_rng(7)
+    x = uniform_complex(rng, (64, 1000), np.complex64)
+    t = torch.from_numpy(x).cuda()
+    ref = np_reference("fft", 0, x)
+    streams = [torch.cuda.Stream() for _ in range(4)]
+    outs = []
+    for s in streams:
+        with torch.cuda.stream(s):
+            outs.append(g.fft("forward", t, stream=s))
+    torch.cuda.synchronize()
+    for o in outs:
+        assert rel_l2(o.cpu().numpy(), ref) < 2e-6
+
+
+def test_fault_injection_alloc(gbfft_lib, monkeypatch):
+    import ctypes
+    from gbfft import _lib as L
+    monkeypatch.setenv("GBFFT_FAULT_INJECT", "alloc")
+    h = ctypes.c_void_p()
+    dims = (ctypes.c_int64 * 1)(1024)
+    assert L.lib().gbfft_plan_create(ctypes.byref(h), 1, dims, 1, 0, 0) == L.ERR_ALLOC
+    assert not h.value
