@@ -1,0 +1,267 @@
+// Strided-axis transform of length 4096 (the column pass of fft2D on a
+// 4096-row array, or any axis of stride S with S a multiple of 16) in one
+// HBM round trip, using an 8-CTA thread-block cluster per 16-column tile.
+//
+// The 4096-point column DFT is split four-step as 64 x 64 (y = 64a + b,
+// k = K + 64k'):
+//   phase 1: CTA r owns b in [8r, 8r+8): DFT-64 over a (as 8 x 8, one smem
+//            exchange), twiddle W_4096^(b*K); result kept in its smem as
+//            [b_local][K][x].
+//   cluster barrier
+//   phase 2: CTA r owns K in [8r, 8r+8): DFT-64 over b, where b = 8*b1 + bl
+//            lives in CTA b1 -- the first radix-8 stage reads one element
+//            from each CTA of the cluster through distributed shared memory;
+//            output rows K + 64k'.
+// Every global access is a 128-byte row segment (16 consecutive columns).
+#include <cooperative_groups.h>
+
+#include "butterflies.cuh"
+#include "gbfft_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace gbfft {
+
+namespace {
+
+template <typename C>
+__device__ __forceinline__ C tw_at(const C* __restrict__ w4096, int t) {
+  return __ldg(w4096 + t);
+}
+
+// v[k] *= base * W_4096^(m*k), k < 8: the powers come from two table entries
+// (W^m, W^4m) with at most two complex multiplications each, applied in
+// place so only four twiddles are live at a time.
+template <typename C>
+__device__ __forceinline__ void apply_powers8(C (&v)[8], const C* __restrict__ w, int m) {
+  const C w1 = tw_at(w, m & 4095);
+  const C w4 = tw_at(w, (4 * m) & 4095);
+  const C w2 = cmul(w1, w1);
+  const C w3 = cmul(w2, w1);
+  v[1] = cmul(v[1], w1);
+  v[2] = cmul(v[2], w2);
+  v[3] = cmul(v[3], w3);
+  v[4] = cmul(v[4], w4);
+  v[5] = cmul(v[5], cmul(w4, w1));
+  v[6] = cmul(v[6], cmul(w4, w2));
+  v[7] = cmul(v[7], cmul(w4, w3));
+}
+template <typename C>
+__device__ __forceinline__ void apply_powers8(C (&v)[8], const C* __restrict__ w, int m, C base) {
+  const C w1 = tw_at(w, m & 4095);
+  const C w4 = tw_at(w, (4 * m) & 4095);
+  const C w2 = cmul(w1, w1);
+  const C w3 = cmul(w2, w1);
+  const C b4 = cmul(base, w4);
+  v[0] = cmul(v[0], base);
+  v[1] = cmul(v[1], cmul(base, w1));
+  v[2] = cmul(v[2], cmul(base, w2));
+  v[3] = cmul(v[3], cmul(base, w3));
+  v[4] = cmul(v[4], b4);
+  v[5] = cmul(v[5], cmul(b4, w1));
+  v[6] = cmul(v[6], cmul(b4, w2));
+  v[7] = cmul(v[7], cmul(b4, w3));
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// address of the same shared-memory location in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t mapa_u32(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float2 ld_dsmem(uint32_t addr, float2*) {
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ double2 ld_dsmem(uint32_t addr, double2*) {
+  double2 v;
+  asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(addr) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void cluster_arrive_release() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait_acquire() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Tile of W columns (8 or 16) per cluster; each thread owns U butterflies
+// (U = 1 or 2) of every radix-8 stage.  Shared layout [g][row][x] with a pad
+// of W elements per g-block (pitch GP) so the half-warps of the W = 8 tile hit
+// distinct banks.
+template <int W> constexpr int col_gp() { return 64 * W + W; }
+
+template <typename T, int W, int U, int MINB>
+__global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(64 * W / U, MINB)
+    colfft4096_kernel(const PassDesc d) {
+  using C = typename CxT<T>::type;
+  constexpr int GP = col_gp<W>();
+  constexpr int HS = 8 / U;  // stride between a thread's butterflies
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sm = reinterpret_cast<C*>(smem_raw);
+  const int r = int(cg::this_cluster().block_rank());
+  const int64_t tile = int64_t(blockIdx.x) >> 3;
+  const int64_t tpb = d.ncols / W;  // W-column tiles per batch
+  const int64_t bo = tile / tpb;
+  const int64_t x0 = (tile - bo * tpb) * W;
+  const C* __restrict__ in = static_cast<const C*>(d.in) + bo * d.in_bs + x0;
+  C* __restrict__ out = static_cast<C*>(d.out) + bo * d.out_bs + x0;
+  const C* __restrict__ w = static_cast<const C*>(d.tw);  // W_4096^t, t < 4096
+  const int64_t ies = d.in_es, oes = d.out_es;
+  const uint32_t fl = d.flags;
+
+  const int tid = threadIdx.x;
+  const int x = tid % W;
+  const int g = (tid / W) & 7;
+  const int h = tid / (8 * W);  // 0 .. HS-1
+  C v[U][8];
+
+  // ---- phase 1, stage A: thread (x, bl = g, a2 in {h + HS*u}) ---------------
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int a2 = h + HS * u;
+#pragma unroll
+    for (int a1 = 0; a1 < 8; ++a1) {
+      const int y = 64 * (8 * a1 + a2) + 8 * r + g;
+      C e = in[int64_t(y) * ies + x];
+      if (fl & F_CONJ_IN) e.y = -e.y;
+      v[u][a1] = e;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int a2 = h + HS * u;
+    dft8(v[u]);
+    apply_powers8(v[u], w, 64 * a2);
+#pragma unroll
+    for (int k1 = 0; k1 < 8; ++k1) sm[g * GP + (a2 * 8 + k1) * W + x] = v[u][k1];
+  }
+  __syncthreads();
+  // ---- stage B: thread (x, bl = g, k1 in {h + HS*u}) -------------------------
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int k1 = h + HS * u;
+#pragma unroll
+    for (int a2 = 0; a2 < 8; ++a2) v[u][a2] = sm[g * GP + (a2 * 8 + k1) * W + x];
+  }
+  __syncthreads();
+  const int b = 8 * r + g;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int k1 = h + HS * u;
+    dft8(v[u]);
+    // W^(b*K) = W^(b*k1) * W^(8*b*k2)
+    apply_powers8(v[u], w, 8 * b, tw_at(w, b * k1));
+#pragma unroll
+    for (int k2 = 0; k2 < 8; ++k2) sm[g * GP + (k1 + 8 * k2) * W + x] = v[u][k2];
+  }
+  cluster_arrive_release();
+  cluster_wait_acquire();
+
+  // ---- phase 2, stage C: thread (x, Kl = g, bl' in {h + HS*u}) ---------------
+  const int K = 8 * r + g;
+  const uint32_t sm0 = smem_u32(sm);
+#pragma unroll
+  for (int b1 = 0; b1 < 8; ++b1) {
+    const uint32_t rs = mapa_u32(sm0, uint32_t(b1));
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int blp = h + HS * u;
+      v[u][b1] = ld_dsmem(rs + uint32_t((blp * GP + K * W + x) * sizeof(C)), (C*)nullptr);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int blp = h + HS * u;
+    dft8(v[u]);
+    apply_powers8(v[u], w, 64 * blp);
+  }
+  // signal that this CTA's reads of the cluster's smem are done (release
+  // orders the remote loads before the arrive), and wait until every CTA's
+  // are before overwriting local smem
+  cluster_arrive_release();
+  cluster_wait_acquire();
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int blp = h + HS * u;
+#pragma unroll
+    for (int kb1 = 0; kb1 < 8; ++kb1) sm[g * GP + (blp * 8 + kb1) * W + x] = v[u][kb1];
+  }
+  __syncthreads();
+  // ---- stage D: thread (x, Kl = g, kb1 in {h + HS*u}) ------------------------
+  const T s = T(d.scale);
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int kb1 = h + HS * u;
+#pragma unroll
+    for (int blp = 0; blp < 8; ++blp) v[u][blp] = sm[g * GP + (blp * 8 + kb1) * W + x];
+    dft8(v[u]);
+#pragma unroll
+    for (int kb2 = 0; kb2 < 8; ++kb2) {
+      C e = v[u][kb2];
+      if (fl & F_SCALE) e = cscale(e, s);
+      if (fl & F_CONJ_OUT) e.y = -e.y;
+      const int row = K + 64 * (kb1 + 8 * kb2);
+      out[int64_t(row) * oes + x] = e;
+    }
+  }
+}
+
+template <typename T, int W> size_t col_smem() { return size_t(8) * col_gp<W>() * sizeof(typename CxT<T>::type); }
+
+template <typename T, int W, int U, int MINB>
+struct ColCfg {
+  static constexpr int threads = 64 * W / U;
+  static cudaError_t prepare() {
+    return cudaFuncSetAttribute(colfft4096_kernel<T, W, U, MINB>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, int(col_smem<T, W>()));
+  }
+  static cudaError_t launch(const PassDesc& d, cudaStream_t s) {
+    const int64_t tiles = (d.ncols / W) * d.nbatch;
+    colfft4096_kernel<T, W, U, MINB><<<unsigned(tiles * 8), threads, col_smem<T, W>(), s>>>(d);
+    return cudaGetLastError();
+  }
+};
+
+// Variants (selected by PassDesc::col_variant):
+//   0: W = 16, U = 2, 512 threads, 2 CTAs/SM
+//   1: W = 8,  U = 1, 512 threads, 3 CTAs/SM
+//   2: W = 8,  U = 2, 256 threads, 4 CTAs/SM
+//   3: W = 16, U = 1, 1024 threads, 1 CTA/SM
+#define GBFFT_COL_TABLE(X) \
+  X(0, float, 16, 2, 2)    \
+  X(1, float, 8, 1, 3)     \
+  X(2, float, 8, 2, 4)     \
+  X(3, float, 16, 1, 1)
+
+}  // namespace
+
+cudaError_t prepare_col_kernels() {
+  cudaError_t e = cudaSuccess;
+#define X(V, T, W, U, MINB) \
+  if (e == cudaSuccess) e = ColCfg<T, W, U, MINB>::prepare();
+  GBFFT_COL_TABLE(X)
+#undef X
+  if (e == cudaSuccess) e = ColCfg<double, 16, 2, 1>::prepare();
+  return e;
+}
+
+int col_tile_width(int variant) {
+  return (variant == 1 || variant == 2) ? 8 : 16;
+}
+
+cudaError_t launch_col4096(const PassDesc& d, bool dbl, cudaStream_t s) {
+  if (dbl) return ColCfg<double, 16, 2, 1>::launch(d, s);
+#define X(V, T, W, U, MINB) \
+  if (d.col_variant == V) return ColCfg<T, W, U, MINB>::launch(d, s);
+  GBFFT_COL_TABLE(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace gbfft

@@ -10,6 +10,10 @@ namespace gbfft {
 
 constexpr int kMaxStages = 16;
 
+// Value a kernel writes into a plan's device status word when a bounded wait
+// gives up (equals GBFFT_ERR_TIMEOUT of the C ABI).
+constexpr int GBFFT_ERR_TIMEOUT_DEVICE = 6;
+
 // Largest transform length one CTA computes in shared memory (two ping-pong
 // buffers of one column each); longer axes are split four-step.
 constexpr int kCapC32 = 8192;
@@ -28,6 +32,13 @@ enum PassFlags : uint32_t {
   F_FILTER_OUT = 1u << 8,  // multiply by filter[l] then conjugate, on store
   F_CHIRP_OUT = 1u << 9,   // conjugate then multiply by chirp[l] on store
   F_TRUNC_OUT = 1u << 10,  // store only logical output index l < n_out
+};
+
+// Kernel families a pass can run on.
+enum KernelId : int {
+  K_PENCIL = 0,   // generic shared-memory pencil kernel (any length <= cap, fused ops)
+  K_ROW = 1,      // register-resident contiguous-row kernel (specialised lengths)
+  K_COL4096 = 2,  // 8-CTA cluster kernel for stride-S axes of length 4096
 };
 
 struct StageInfo {
@@ -55,6 +66,11 @@ struct PassDesc {
   int load_cfast;   // 1: loads map consecutive threads to consecutive columns
   int store_cfast;  // 1: stores map consecutive threads to consecutive columns
   uint32_t flags;
+  int kernel;   // KernelId
+  int use_tma;  // K_ROW: stream chunks with cp.async.bulk when the layout allows
+  int row_variant;  // K_ROW: 0 double-buffered exchanges, 1 single buffer (more CTAs/SM)
+  int col_variant;  // K_COL4096: tile width / threads variant (colfft.cu)
+  int* status;  // device status word of the plan (0 = ok)
   StageInfo st[kMaxStages];
   const void* tw;  // stage twiddles (element type of the pass)
   double scale;
@@ -79,5 +95,12 @@ cudaError_t launch_pass(const PassDesc& d, bool is_double, cudaStream_t stream);
 
 // Prepare kernel attributes (max dynamic shared memory); idempotent.
 cudaError_t prepare_kernels();
+
+bool row_kernel_available(int n, bool dbl);
+cudaError_t prepare_row_kernels();
+cudaError_t launch_row(const PassDesc& d, bool dbl, cudaStream_t s);
+cudaError_t prepare_col_kernels();
+cudaError_t launch_col4096(const PassDesc& d, bool dbl, cudaStream_t s);
+int col_tile_width(int variant);
 
 }  // namespace gbfft

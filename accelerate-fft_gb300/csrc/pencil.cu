@@ -20,7 +20,8 @@ __device__ __forceinline__ C ldg_c(const C* p) {
 
 // One Stockham stage of radix R over every pencil of the tile:
 // butterfly j reads src[j + r*n/R], twiddles by W_{Ns*R}^{(j mod Ns)*r},
-// and writes dst[(j/Ns)*Ns*R + (j mod Ns) + r*Ns].
+// and writes dst[(j/Ns)*Ns*R + (j mod Ns) + r*Ns].  The stage twiddle table
+// holds W_{Ns*R}^{p*r} at p*Rp + r, Rp = R rounded up to even.
 template <int R, typename C>
 __device__ __forceinline__ void stage(const C* __restrict__ src, C* __restrict__ dst,
                                       const C* __restrict__ tw, int n, int Ns, int W, int pitch) {
@@ -36,9 +37,9 @@ __device__ __forceinline__ void stage(const C* __restrict__ src, C* __restrict__
     for (int r = 0; r < R; ++r) v[r] = s[spad(j + r * nb)];
     const int p = j % Ns;
     if (Ns > 1) {
-      const C* t = tw + p * (R - 1);
+      const C* t = tw + p * (R + (R & 1));
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], ldg_c(t + r - 1));
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], ldg_c(t + r));
     }
     dft<R>(v);
     const int base = (j - p) * R + p;
@@ -178,7 +179,11 @@ int pass_grid(const PassDesc& d) {
 
 // Applies to the current device; called at every plan creation.
 cudaError_t prepare_kernels() {
-  cudaError_t e = cudaFuncSetAttribute(pencil_kernel<float>,
+  cudaError_t e = prepare_row_kernels();
+  if (e != cudaSuccess) return e;
+  e = prepare_col_kernels();
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(pencil_kernel<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(pencil_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -186,6 +191,8 @@ cudaError_t prepare_kernels() {
 }
 
 cudaError_t launch_pass(const PassDesc& d, bool is_double, cudaStream_t stream) {
+  if (d.kernel == K_ROW) return launch_row(d, is_double, stream);
+  if (d.kernel == K_COL4096) return launch_col4096(d, is_double, stream);
   const int grid = pass_grid(d);
   if (grid <= 0) return cudaSuccess;
   const size_t smem = pass_smem_bytes(d, is_double);

@@ -169,8 +169,9 @@ bool Builder::stages_for(int n, PassSpec& ps) {
     for (size_t s = 0; s < f.size(); ++s) {
       offs[s] = int(t.size());
       const int R = f[s];
+      const int Rp = R + (R & 1);  // even stride: each butterfly's twiddles start 16-byte aligned
       for (int64_t p = 0; p < Ns; ++p)
-        for (int r = 1; r < R; ++r) t.push_back(unit_root(p * r, Ns * R));
+        for (int r = 0; r < Rp; ++r) t.push_back(unit_root(p * r, Ns * R));
       Ns *= R;
     }
     if (t.empty()) t.push_back(cd(1, 0));
@@ -238,6 +239,16 @@ void Builder::blue_for(int64_t n, int64_t m, PassSpec& ps) {
   }
   ps.chirp_off = int64_t(it->second.chirp);
   ps.filter_off = int64_t(it->second.filter);
+}
+
+size_t Builder::roots_for(int64_t N) {
+  auto it = roots_cache.find(N);
+  if (it != roots_cache.end()) return it->second;
+  std::vector<cd> t(static_cast<size_t>(N));
+  for (int64_t i = 0; i < N; ++i) t[size_t(i)] = unit_root(i, N);
+  const size_t off = add(t);
+  roots_cache.emplace(N, off);
+  return off;
 }
 
 void choose_tile(PassSpec& ps, bool dbl) {
@@ -321,10 +332,22 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     d.ncols = ax.ncols;
     d.nbatch = d.nb_lo = ax.outer;
     choose_tile(ps, dbl);
+    const char* kname = "pencil";
+    if (ax.es == 1 && ax.outer == 1 && row_kernel_available(int(ax.n), dbl) &&
+        !feature_disabled("row")) {
+      d.kernel = K_ROW;
+      kname = "row";
+    } else if (ax.n == 4096 && ax.cs == 1 && ax.es != 1 && ax.ncols % (dbl ? 16 : 8) == 0 &&
+               !feature_disabled("cluster")) {
+      d.kernel = K_COL4096;
+      ps.tw_off = int64_t(B.roots_for(4096));
+      kname = "col4096-cluster8";
+    }
     ps.src = src;
     ps.dst = R_OUT;
     passes.push_back(ps);
-    std::snprintf(buf, sizeof buf, "[n=%lld es=%lld W=%d]", (long long)ax.n, (long long)ax.es, ps.d.W);
+    std::snprintf(buf, sizeof buf, "[n=%lld es=%lld %s W=%d]", (long long)ax.n, (long long)ax.es,
+                  kname, ps.d.W);
     desc += buf;
     return GBFFT_OK;
   }
@@ -511,6 +534,11 @@ bool fault_injected(const char* what) {
   return e && std::strstr(e, what) != nullptr;
 }
 
+bool feature_disabled(const char* what) {
+  const char* e = std::getenv("GBFFT_DISABLE");
+  return e && std::strstr(e, what) != nullptr;
+}
+
 }  // namespace gbfft
 
 using namespace gbfft;
@@ -556,6 +584,8 @@ int build_plan(gbfft_plan* p, bool dry) {
     if (st != GBFFT_OK) return st;
     if (p->passes.size() > before) first = false;
   }
+  // device status word (zero) at the head of the tables
+  const size_t status_off = B.add(std::vector<cd>(2, cd(0, 0)));
   // device tables
   const size_t eb = p->dbl ? 16 : 8;
   if (dry) {
@@ -578,7 +608,19 @@ int build_plan(gbfft_plan* p, bool dry) {
     if (cudaMalloc(&p->d_scratch, p->scratch_bytes) != cudaSuccess) return GBFFT_ERR_ALLOC;
   }
   unsigned char* base = static_cast<unsigned char*>(p->d_tables);
+  p->d_status = reinterpret_cast<int*>(base + status_off);
+  const bool tma = !feature_disabled("tma");
   for (PassSpec& ps : p->passes) {
+    ps.d.status = p->d_status;
+    ps.d.use_tma = tma ? 1 : 0;
+    // measured defaults on GB300 (fft2D 4096^2): single-buffered rows at
+    // 4 CTAs/SM, 8-column cluster tiles at 4 CTAs/SM; env overrides for A/B
+    ps.d.row_variant = 1;
+    ps.d.col_variant = 2;
+    if (const char* rv = std::getenv("GBFFT_ROW_VARIANT")) ps.d.row_variant = std::atoi(rv) & 1;
+    if (const char* cv = std::getenv("GBFFT_COL_VARIANT")) ps.d.col_variant = std::atoi(cv) & 3;
+    if (ps.d.kernel == K_COL4096 && ps.d.ncols % col_tile_width(ps.d.col_variant) != 0)
+      ps.d.col_variant = 1;  // 8-column tiles
     if (ps.tw_off >= 0) ps.d.tw = base + ps.tw_off;
     if (ps.tw4lo_off >= 0) ps.d.tw4_lo = base + ps.tw4lo_off;
     if (ps.tw4hi_off >= 0) ps.d.tw4_hi = base + ps.tw4hi_off;
@@ -841,6 +883,18 @@ int gbfft_exec_range(const gbfft_plan* plan, int mode, int first, int count, con
       return GBFFT_ERR_CUDA;
   }
   return GBFFT_OK;
+}
+
+int gbfft_exec_status(const gbfft_plan* plan, void* stream) {
+  if (!plan) return GBFFT_ERR_NULL_PLAN;
+  if (!plan->d_status) return GBFFT_OK;
+  int h = 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (cudaMemcpyAsync(&h, plan->d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return GBFFT_ERR_CUDA;
+  if (h != 0) cudaMemsetAsync(plan->d_status, 0, sizeof(int), s);
+  return h;
 }
 
 int gbfft_plan_info(const gbfft_plan* plan, size_t* workspace_bytes, int* launches_per_exec) {

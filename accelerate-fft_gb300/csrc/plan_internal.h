@@ -45,11 +45,13 @@ struct Builder {
   std::map<int64_t, StageTable> stage_cache;
   std::map<int64_t, Tw4> tw4_cache;
   std::map<std::pair<int64_t, int64_t>, Blue> blue_cache;
+  std::map<int64_t, size_t> roots_cache;
 
   size_t add(const std::vector<cd>& v);
   bool stages_for(int n, PassSpec& ps);
   void tw4_for(int64_t N, PassSpec& ps);
   void blue_for(int64_t n, int64_t m, PassSpec& ps);
+  size_t roots_for(int64_t N);  // table of W_N^t, t < N
 };
 
 cd unit_root(int64_t t, int64_t L);  // exp(-2*pi*i*t/L), exact reduction
@@ -58,7 +60,8 @@ bool is_fast_length(int64_t n);
 int64_t bluestein_length(int64_t n);
 void host_fft_fp64(std::vector<cd>& x);
 void choose_tile(PassSpec& ps, bool dbl);
-bool fault_injected(const char* what);
+bool fault_injected(const char* what);   // GBFFT_FAULT_INJECT=alloc,...
+bool feature_disabled(const char* what);  // GBFFT_DISABLE=tma,row,cluster (A/B checks)
 
 }  // namespace gbfft
 
@@ -77,6 +80,7 @@ struct gbfft_plan {
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
   size_t s2_off = 0;
+  int* d_status = nullptr;  // device status word inside d_tables
   std::string desc;
 };
 

@@ -1,0 +1,496 @@
+// Register-resident Stockham transform of contiguous rows (the innermost
+// axis: fft / fft1D, and the first pass of fft2D / fft3D).
+//
+// Each row of N elements is owned by TH = N/E threads holding E elements
+// each in registers.  Stage s of radix R gives every thread E/R butterflies
+// j = t + TH*q.  Shared memory only carries the exchanges between stages;
+// exchanges use an XOR swizzle (bits 1-3 of the element index flipped by
+// bits 4-6) that keeps every access pattern of these stages conflict-free and
+// keeps element pairs adjacent, so the first stage's outputs are written as
+// 16-byte vectors.  The radix list is a template parameter equal to the
+// planner's factorisation (factor_device), so both kernels share the stage
+// twiddle table layout of the generic pencil kernel.
+//
+// Two variants:
+//  * rowfft_kernel: one chunk of ROWS rows per CTA, the first stage loading
+//    x[t + TH*m] straight from global memory.
+//  * rowfft_tma_kernel (Complex Float): persistent CTAs; a chunk of ROWS
+//    contiguous rows is fetched into shared memory by one cp.async.bulk
+//    (TMA) completing on an mbarrier, double buffered, so the next chunk
+//    streams in while the current one is transformed.  Waits are bounded: on
+//    timeout the kernel records GBFFT_ERR_TIMEOUT in the plan's status word
+//    and stops.
+#include <algorithm>
+
+#include "butterflies.cuh"
+#include "gbfft_internal.h"
+
+namespace gbfft {
+
+namespace {
+
+__device__ __forceinline__ int swz(int i) { return i ^ (((i >> 4) & 7) << 1); }
+
+template <int... Rs> struct RL {};
+template <int R, int... Rest> constexpr int rl_first(RL<R, Rest...>) { return R; }
+template <int R> constexpr int rl_last(RL<R>) { return R; }
+template <int R, int R2, int... Rest> constexpr int rl_last(RL<R, R2, Rest...>) {
+  return rl_last(RL<R2, Rest...>{});
+}
+template <int R> constexpr int even_up() { return R + (R & 1); }
+// row pitch of the exchange buffers: a multiple of 16 so the swizzle stays
+// inside the row and 16-byte stores stay aligned
+template <int N> constexpr int row_pitch() { return (N + 15) & ~15; }
+
+// twiddles W^{p*r}, r < R, of one butterfly (table stride even_up(R))
+template <int R>
+__device__ __forceinline__ void load_tw(float2 (&w)[R + 1], const float2* __restrict__ base) {
+  const float4* b4 = reinterpret_cast<const float4*>(base);
+#pragma unroll
+  for (int k = 0; k < even_up<R>() / 2; ++k) {
+    const float4 q = __ldg(b4 + k);
+    w[2 * k] = make_float2(q.x, q.y);
+    if (2 * k + 1 <= R) w[2 * k + 1] = make_float2(q.z, q.w);
+  }
+}
+template <int R>
+__device__ __forceinline__ void load_tw(double2 (&w)[R + 1], const double2* __restrict__ base) {
+#pragma unroll
+  for (int r = 1; r < R; ++r) w[r] = __ldg(base + r);
+}
+
+// Complex Float twiddles derived from a few table entries: W^p, W^4p, W^8p
+// are loaded and the other powers formed with at most three complex
+// multiplications (a few ulp), which keeps the L1 traffic per butterfly at
+// three 8-byte loads instead of R-1.
+template <int R>
+__device__ __forceinline__ void derive_tw(float2 (&w)[R + 1], const float2* __restrict__ base) {
+  if constexpr (R == 16) {
+    w[1] = __ldg(base + 1);
+    w[4] = __ldg(base + 4);
+    w[8] = __ldg(base + 8);
+    w[2] = cmul(w[1], w[1]);
+    w[3] = cmul(w[2], w[1]);
+    w[5] = cmul(w[4], w[1]);
+    w[6] = cmul(w[4], w[2]);
+    w[7] = cmul(w[4], w[3]);
+    w[9] = cmul(w[8], w[1]);
+    w[10] = cmul(w[8], w[2]);
+    w[11] = cmul(w[8], w[3]);
+    w[12] = cmul(w[8], w[4]);
+    w[13] = cmul(w[12], w[1]);
+    w[14] = cmul(w[12], w[2]);
+    w[15] = cmul(w[12], w[3]);
+  } else if constexpr (R == 8) {
+    w[1] = __ldg(base + 1);
+    w[4] = __ldg(base + 4);
+    w[2] = cmul(w[1], w[1]);
+    w[3] = cmul(w[2], w[1]);
+    w[5] = cmul(w[4], w[1]);
+    w[6] = cmul(w[4], w[2]);
+    w[7] = cmul(w[4], w[3]);
+  } else {
+    load_tw<R>(w, base);
+  }
+}
+
+template <int N, int E, int NS, int R, typename C>
+__device__ __forceinline__ void row_compute(C (&v)[E], const C* __restrict__ tw, int t) {
+  constexpr int TH = N / E;
+  constexpr int Q = E / R;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    if constexpr (NS > 1) {
+      const int j = t + TH * q;
+      const int p = j % NS;
+      C w[R + 1];
+      if constexpr (sizeof(C) == 8)
+        derive_tw<R>(w, tw + p * even_up<R>());
+      else
+        load_tw<R>(w, tw + p * even_up<R>());
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[q * R + r] = cmul(v[q * R + r], w[r]);
+    }
+    dft<R>(&v[q * R]);
+  }
+}
+
+// After stage (NS, R): outputs go to smem in Stockham order (swizzled).
+template <int N, int E, int NS, int R, typename C>
+__device__ __forceinline__ void row_write(const C (&v)[E], C* buf, int t) {
+  constexpr int TH = N / E;
+  constexpr int Q = E / R;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int j = t + TH * q;
+    if constexpr (NS == 1 && (R % 2 == 0) && sizeof(C) == 8) {
+      // R consecutive outputs j*R + r: store as 16-byte pairs
+#pragma unroll
+      for (int r = 0; r < R; r += 2) {
+        const int i = swz(j * R + r);
+        *reinterpret_cast<float4*>(buf + i) =
+            make_float4(v[q * R + r].x, v[q * R + r].y, v[q * R + r + 1].x, v[q * R + r + 1].y);
+      }
+    } else {
+      const int p = j % NS;
+      const int base = (j - p) * R + p;
+#pragma unroll
+      for (int r = 0; r < R; ++r) buf[swz(base + r * NS)] = v[q * R + r];
+    }
+  }
+}
+
+// Before a stage of radix R: v[q*R + r] = element j_q + r*N/R.
+template <int N, int E, int R, typename C>
+__device__ __forceinline__ void row_read(C (&v)[E], const C* buf, int t) {
+  constexpr int TH = N / E;
+  constexpr int Q = E / R;
+#pragma unroll
+  for (int q = 0; q < Q; ++q)
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[q * R + r] = buf[swz(t + TH * q + r * (N / R))];
+}
+
+// Double-buffered exchanges (bufs = 2 regions of PITCH elements).
+template <int N, int E, int NS, int OFF, int BUF, int PITCH, typename C, int R, int... Rest>
+__device__ __forceinline__ void row_stages2(C (&v)[E], C* bufs, const C* __restrict__ tw, int t,
+                                            RL<R, Rest...>) {
+  row_compute<N, E, NS, R>(v, tw + OFF, t);
+  if constexpr (sizeof...(Rest) > 0) {
+    C* b = bufs + BUF * PITCH;
+    row_write<N, E, NS, R>(v, b, t);
+    __syncthreads();
+    constexpr int R2 = rl_first(RL<Rest...>{});
+    row_read<N, E, R2>(v, b, t);
+    row_stages2<N, E, NS * R, OFF + NS * even_up<R>(), 1 - BUF, PITCH>(v, bufs, tw, t, RL<Rest...>{});
+  }
+}
+
+// Single-buffered exchanges in `b` (two barriers per exchange); ends with a
+// barrier after the last read so the caller may reuse `b`.
+template <int N, int E, int NS, int OFF, typename C, int R, int... Rest>
+__device__ __forceinline__ void row_stages1(C (&v)[E], C* b, const C* __restrict__ tw, int t,
+                                            RL<R, Rest...>) {
+  row_compute<N, E, NS, R>(v, tw + OFF, t);
+  if constexpr (sizeof...(Rest) > 0) {
+    row_write<N, E, NS, R>(v, b, t);
+    __syncthreads();
+    constexpr int R2 = rl_first(RL<Rest...>{});
+    row_read<N, E, R2>(v, b, t);
+    __syncthreads();
+    row_stages1<N, E, NS * R, OFF + NS * even_up<R>()>(v, b, tw, t, RL<Rest...>{});
+  }
+}
+
+template <typename T, int N, int E, int ROWS, int MINB, int... Rs>
+__global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_kernel(const PassDesc d) {
+  using C = typename CxT<T>::type;
+  constexpr int TH = N / E;
+  constexpr int R0 = rl_first(RL<Rs...>{});
+  constexpr int RZ = rl_last(RL<Rs...>{});
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int slot = threadIdx.x / TH;
+  const int t = threadIdx.x - slot * TH;
+  // two exchange regions of ROWS rows; row `slot` at offset slot*row_pitch
+  C* bufs = reinterpret_cast<C*>(smem_raw) + slot * row_pitch<N>();
+  const int64_t row = int64_t(blockIdx.x) * ROWS + slot;
+  const bool ok = row < d.ncols;
+  const uint32_t fl = d.flags;
+  const C* __restrict__ in = static_cast<const C*>(d.in) + row * d.in_cs;
+  C* __restrict__ out = static_cast<C*>(d.out) + row * d.out_cs;
+
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < E / R0; ++q)
+#pragma unroll
+    for (int r = 0; r < R0; ++r) {
+      C x = cmake<C>(T(0), T(0));
+      if (ok) x = in[t + TH * (q + r * (E / R0))];
+      if (fl & F_CONJ_IN) x.y = -x.y;
+      v[q * R0 + r] = x;
+    }
+  row_stages2<N, E, 1, 0, 0, ROWS * row_pitch<N>()>(v, bufs, static_cast<const C*>(d.tw), t,
+                                                   RL<Rs...>{});
+  if (!ok) return;
+  const T s = T(d.scale);
+#pragma unroll
+  for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+    for (int r = 0; r < RZ; ++r) {
+      C x = v[q * RZ + r];
+      if (fl & F_SCALE) x = cscale(x, s);
+      if (fl & F_CONJ_OUT) x.y = -x.y;
+      out[t + TH * (q + r * (E / RZ))] = x;
+    }
+}
+
+// Variant with one exchange buffer (half the shared memory, two barriers per
+// exchange) so more CTAs fit on an SM.
+template <typename T, int N, int E, int ROWS, int MINB, int... Rs>
+__global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft1_kernel(const PassDesc d) {
+  using C = typename CxT<T>::type;
+  constexpr int TH = N / E;
+  constexpr int R0 = rl_first(RL<Rs...>{});
+  constexpr int RZ = rl_last(RL<Rs...>{});
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int slot = threadIdx.x / TH;
+  const int t = threadIdx.x - slot * TH;
+  C* b = reinterpret_cast<C*>(smem_raw) + slot * row_pitch<N>();
+  const int64_t row = int64_t(blockIdx.x) * ROWS + slot;
+  const bool ok = row < d.ncols;
+  const uint32_t fl = d.flags;
+  const C* __restrict__ in = static_cast<const C*>(d.in) + row * d.in_cs;
+  C* __restrict__ out = static_cast<C*>(d.out) + row * d.out_cs;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < E / R0; ++q)
+#pragma unroll
+    for (int r = 0; r < R0; ++r) {
+      C x = cmake<C>(T(0), T(0));
+      if (ok) x = in[t + TH * (q + r * (E / R0))];
+      if (fl & F_CONJ_IN) x.y = -x.y;
+      v[q * R0 + r] = x;
+    }
+  row_stages1<N, E, 1, 0>(v, b, static_cast<const C*>(d.tw), t, RL<Rs...>{});
+  if (!ok) return;
+  const T s = T(d.scale);
+#pragma unroll
+  for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+    for (int r = 0; r < RZ; ++r) {
+      C x = v[q * RZ + r];
+      if (fl & F_SCALE) x = cscale(x, s);
+      if (fl & F_CONJ_OUT) x.y = -x.y;
+      out[t + TH * (q + r * (E / RZ))] = x;
+    }
+}
+
+// ---- TMA-fed persistent variant (Complex Float) ----------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+constexpr uint32_t kWaitLimit = 1u << 22;  // try_wait polls before giving up
+
+// Bounded wait; returns false (and records a timeout) if it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
+  for (uint32_t it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (status) atomicExch(status, GBFFT_ERR_TIMEOUT_DEVICE);
+  return false;
+}
+
+template <int N, int E, int ROWS, int MINB, int... Rs>
+__global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_tma_kernel(const PassDesc d) {
+  using C = float2;
+  constexpr int TH = N / E;
+  constexpr int CH = ROWS * N;
+  constexpr int R0 = rl_first(RL<Rs...>{});
+  constexpr int RZ = rl_last(RL<Rs...>{});
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars[2];
+  C* buf0 = reinterpret_cast<C*>(smem_raw);
+  const int slot = threadIdx.x / TH;
+  const int t = threadIdx.x - slot * TH;
+  const int64_t rows = d.ncols;
+  const int64_t nchunks = (rows + ROWS - 1) / ROWS;
+  const C* __restrict__ in = static_cast<const C*>(d.in);
+  C* __restrict__ out = static_cast<C*>(d.out);
+  const C* __restrict__ tw = static_cast<const C*>(d.tw);
+  const uint32_t fl = d.flags;
+  const float s = float(d.scale);
+
+  auto issue = [&](int64_t c, int b) {
+    const int64_t r0 = c * ROWS;
+    const int64_t nr = (rows - r0 < ROWS) ? rows - r0 : ROWS;
+    const uint32_t bytes = uint32_t(nr * N * sizeof(C));
+    mbar_expect_tx(&bars[b], bytes);
+    tma_load_1d(buf0 + b * CH, in + r0 * N, bytes, &bars[b]);
+  };
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 2; ++k) {
+      const int64_t c = int64_t(blockIdx.x) + int64_t(k) * gridDim.x;
+      if (c < nchunks) issue(c, k);
+    }
+  }
+  int it = 0;
+  for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x, ++it) {
+    const int b = it & 1;
+    const uint32_t par = uint32_t(it >> 1) & 1u;
+    // every thread observes the completed phase (acquire) before reading;
+    // the abort decision is made uniformly across the CTA
+    const bool timed_out = !mbar_wait_bounded(&bars[b], par, d.status);
+    if (__syncthreads_or(timed_out)) break;
+    C* sb = buf0 + b * CH + slot * N;
+    const int64_t row = c * ROWS + slot;
+    const bool ok = row < rows;
+    C v[E];
+#pragma unroll
+    for (int q = 0; q < E / R0; ++q)
+#pragma unroll
+      for (int r = 0; r < R0; ++r) {
+        C x = sb[t + TH * (q + r * (E / R0))];
+        if (fl & F_CONJ_IN) x.y = -x.y;
+        v[q * R0 + r] = x;
+      }
+    __syncthreads();  // stage-1 inputs consumed; the chunk buffer becomes the exchange buffer
+    row_stages1<N, E, 1, 0>(v, sb, tw, t, RL<Rs...>{});
+    // the buffer is free again: prefetch the chunk after next into it
+    if (threadIdx.x == 0) {
+      const int64_t cn = c + 2 * int64_t(gridDim.x);
+      fence_async_smem();
+      if (cn < nchunks) issue(cn, b);
+    }
+    if (ok) {
+      C* o = out + row * N;
+#pragma unroll
+      for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+        for (int r = 0; r < RZ; ++r) {
+          C x = v[q * RZ + r];
+          if (fl & F_SCALE) x = cscale(x, s);
+          if (fl & F_CONJ_OUT) x.y = -x.y;
+          o[t + TH * (q + r * (E / RZ))] = x;
+        }
+    }
+  }
+  // drain: do not exit with a bulk copy still targeting this CTA's smem
+  if (threadIdx.x == 0) {
+    int it2 = it;
+    for (int k = 0; k < 2; ++k, ++it2) {
+      const int64_t c = int64_t(blockIdx.x) + int64_t(it2) * gridDim.x;
+      if (c < nchunks) mbar_wait_bounded(&bars[it2 & 1], uint32_t(it2 >> 1) & 1u, d.status);
+    }
+  }
+}
+
+template <typename T, int N, int E, int ROWS, int MINB, int... Rs>
+struct RowCfg {
+  static constexpr int threads = ROWS * (N / E);
+  static constexpr bool tma_capable = sizeof(T) == 4 && N % 16 == 0;
+  static size_t smem() { return size_t(2) * ROWS * row_pitch<N>() * sizeof(typename CxT<T>::type); }
+  static int tma_ctas_per_sm;
+  static constexpr int MINB1 = (MINB >= 3 && sizeof(T) == 4) ? 4 : MINB;
+  static cudaError_t prepare() {
+    cudaError_t e = cudaFuncSetAttribute(rowfft_kernel<T, N, E, ROWS, MINB, Rs...>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem()));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(rowfft1_kernel<T, N, E, ROWS, MINB1, Rs...>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem() / 2));
+    if constexpr (tma_capable) {
+      if (e != cudaSuccess) return e;
+      e = cudaFuncSetAttribute(rowfft_tma_kernel<N, E, ROWS, MINB, Rs...>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem()));
+      if (e != cudaSuccess) return e;
+      int nb = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rowfft_tma_kernel<N, E, ROWS, MINB, Rs...>,
+                                                        threads, smem());
+      tma_ctas_per_sm = nb > 0 ? nb : 1;
+    }
+    return e;
+  }
+  static cudaError_t launch(const PassDesc& d, cudaStream_t s, int sms) {
+    const int64_t chunks = (d.ncols + ROWS - 1) / ROWS;
+    if (d.row_variant & 1) {
+      rowfft1_kernel<T, N, E, ROWS, MINB1, Rs...><<<unsigned(chunks), threads, smem() / 2, s>>>(d);
+      return cudaGetLastError();
+    }
+    if constexpr (tma_capable) {
+      const bool tma_ok = d.in_cs == N && d.out_cs == N &&
+                          (reinterpret_cast<uintptr_t>(d.in) & 15) == 0 && d.use_tma;
+      if (tma_ok) {
+        const int64_t grid = std::min<int64_t>(chunks, int64_t(sms) * tma_ctas_per_sm);
+        rowfft_tma_kernel<N, E, ROWS, MINB, Rs...><<<unsigned(grid), threads, smem(), s>>>(d);
+        return cudaGetLastError();
+      }
+    }
+    rowfft_kernel<T, N, E, ROWS, MINB, Rs...><<<unsigned(chunks), threads, smem(), s>>>(d);
+    return cudaGetLastError();
+  }
+};
+template <typename T, int N, int E, int ROWS, int MINB, int... Rs>
+int RowCfg<T, N, E, ROWS, MINB, Rs...>::tma_ctas_per_sm = 1;
+
+// The specialised lengths (type, N, E, rows per CTA, min CTAs per SM,
+// radices = factor_device(N)).
+#define GBFFT_ROW_TABLE(X)                   \
+  X(float, 256, 16, 16, 3, 16, 16)           \
+  X(float, 512, 16, 8, 3, 16, 16, 2)         \
+  X(float, 1024, 16, 4, 3, 16, 16, 4)        \
+  X(float, 2048, 16, 2, 3, 16, 16, 8)        \
+  X(float, 4096, 16, 1, 3, 16, 16, 16)       \
+  X(float, 8192, 16, 1, 1, 16, 16, 16, 2)    \
+  X(float, 1000, 40, 4, 2, 8, 5, 5, 5)       \
+  X(double, 256, 16, 16, 2, 16, 16)          \
+  X(double, 512, 16, 8, 2, 16, 16, 2)        \
+  X(double, 1024, 16, 4, 2, 16, 16, 4)       \
+  X(double, 2048, 16, 2, 1, 16, 16, 8)       \
+  X(double, 4096, 16, 1, 1, 16, 16, 16)
+
+int g_sms = 0;
+
+}  // namespace
+
+bool row_kernel_available(int n, bool dbl) {
+#define X(T, N, E, ROWS, MINB, ...) \
+  if (n == N && dbl == (sizeof(T) == 8)) return true;
+  GBFFT_ROW_TABLE(X)
+#undef X
+  return false;
+}
+
+cudaError_t prepare_row_kernels() {
+  cudaError_t e = cudaSuccess;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+#define X(T, N, E, ROWS, MINB, ...) \
+  if (e == cudaSuccess) e = RowCfg<T, N, E, ROWS, MINB, __VA_ARGS__>::prepare();
+  GBFFT_ROW_TABLE(X)
+#undef X
+  return e;
+}
+
+cudaError_t launch_row(const PassDesc& d, bool dbl, cudaStream_t s) {
+  const int sms = g_sms > 0 ? g_sms : 1;
+#define X(T, N, E, ROWS, MINB, ...) \
+  if (d.n == N && dbl == (sizeof(T) == 8)) return RowCfg<T, N, E, ROWS, MINB, __VA_ARGS__>::launch(d, s, sms);
+  GBFFT_ROW_TABLE(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace gbfft

@@ -40,6 +40,7 @@ SIGNATURES = {
     "gbfft_fft": (_i, [_i, _i, _i64p, _i, _i, _vp, _vp, _vp]),
     "gbfft_cache_clear": (_i, []),
     "gbfft_exec_range": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp]),
+    "gbfft_exec_status": (_i, [_vp, _vp]),
     "gbfft_plan_info": (_i, [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_i)]),
     "gbfft_plan_describe": (_i, [_vp, ctypes.c_char_p, _sz]),
     "gbfft_plan_explain": (_i, [_i, _i64p, _i, _i, _i, ctypes.c_char_p, _sz]),

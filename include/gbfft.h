@@ -103,6 +103,11 @@ int gbfft_fft(int mode, int rank, const int64_t* dims, int kind, int dtype, cons
  * hook of PTX/Plans.hs:79-80). */
 int gbfft_cache_clear(void);
 
+/* Device-side status of the plan's earlier execs on `stream`: GBFFT_OK, or
+ * GBFFT_ERR_TIMEOUT if a bounded wait inside a kernel gave up (the status is
+ * then cleared).  Synchronises the stream. */
+int gbfft_exec_status(const gbfft_plan* plan, void* stream);
+
 /* Instrumentation: run passes [first, first+count) of the plan only, with
  * the same buffers and mode handling as gbfft_exec (running every range in
  * order equals one gbfft_exec).  Lets a profiler time each pass. */

@@ -283,3 +283,47 @@ def test_fault_injection_alloc(gbfft_lib, monkeypatch):
     dims = (ctypes.c_int64 * 1)(1024)
     assert L.lib().gbfft_plan_create(ctypes.byref(h), 1, dims, 1, 0, 0) == L.ERR_ALLOC
     assert not h.value
+
+
+# ---- kernel variants: TMA-fed rows, register rows, cluster columns, generic --
+@pytest.mark.parametrize("disable,rowv,colv", [("", "1", "2"), ("", "0", "0"), ("tma", "0", "1"),
+                                               ("", "1", "3"), ("row", "1", "2"), ("cluster", "1", "2"),
+                                               ("tma,row,cluster", "0", "0")])
+def test_kernel_variants_agree(gbfft_lib, monkeypatch, disable, rowv, colv):
+    g = gbfft_lib
+    from gbfft import _lib as L
+    monkeypatch.setenv("GBFFT_DISABLE", disable)
+    monkeypatch.setenv("GBFFT_ROW_VARIANT", rowv)
+    monkeypatch.setenv("GBFFT_COL_VARIANT", colv)
+    rng = np.random.default_rng(99)
+    cases = [((4096, 4096), "full", np.complex64), ((300, 1024), "many", np.complex64),
+             ((64, 1000), "many", np.complex64), ((5, 8192), "many", np.complex64),
+             ((41, 256), "many", np.complex64), ((3, 2048), "full", np.complex64),
+             ((7, 512), "many", np.complex64), ((33, 4096), "many", np.complex128),
+             ((2, 4096, 32), "full", np.complex64)]
+    for shape, kind, dt in cases:
+        x = uniform_complex(rng, shape, dt)
+        plan = g.Plan(shape, kind=kind, dtype=torch.complex64 if dt == np.complex64 else torch.complex128)
+        for mode in MODES:
+            y = plan(mode, torch.from_numpy(x).cuda()).cpu().numpy()
+            ref = np_reference("fft2D" if kind == "full" else "fft", MODE_IDX[mode], x) if len(shape) == 2 \
+                else np_reference("fft3D" if kind == "full" else "fft", MODE_IDX[mode], x)
+            assert rel_l2(y, ref) < tol_fp64(dt, shape), (shape, kind, mode, disable, plan.describe())
+        assert L.lib().gbfft_exec_status(plan.handle, None) == 0
+        plan.close()
+
+
+def test_row_kernel_input_not_16_byte_aligned(gbfft_lib):
+    # an 8-byte-aligned view: the TMA bulk copy needs 16 bytes, the planner
+    # falls back to direct loads
+    g = gbfft_lib
+    rng = np.random.default_rng(5)
+    rows, n = 64, 4096
+    base = torch.from_numpy(uniform_complex(rng, (rows * n + 1,), np.complex64)).cuda()
+    view = base[1:].view(rows, n)
+    assert view.data_ptr() % 16 == 8
+    plan = g.Plan((rows, n), kind="many", dtype=torch.complex64)
+    out = torch.empty((rows, n), dtype=torch.complex64, device="cuda")
+    plan.exec_ptr("forward", view.data_ptr(), out.data_ptr())
+    ref = np.fft.fft(view.cpu().numpy().astype(np.complex128), axis=-1)
+    assert rel_l2(out.cpu().numpy(), ref) < 2e-6
