@@ -83,6 +83,9 @@ struct PassDesc {
   int tw4_shift;
   const void* tw4_lo;
   const void* tw4_hi;
+  int src_role, dst_role;      // buffer roles (ragged executor)
+  const int64_t* col_in_off;   // optional per-column element offsets (ragged groups)
+  const int64_t* col_out_off;
   const void* chirp;   // Bluestein chirp c[l] = exp(-i*pi*l^2/n), l < n
   const void* filter;  // Bluestein filter spectrum DFT(conj chirp)/m, length m
 };

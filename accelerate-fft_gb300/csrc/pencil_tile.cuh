@@ -1,0 +1,173 @@
+// Device body of the generic pencil pass (shared by the per-pass kernel and
+// the persistent ragged-batch executor).
+#pragma once
+
+#include "butterflies.cuh"
+#include "gbfft_internal.h"
+
+namespace gbfft {
+
+__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
+
+template <typename C>
+__device__ __forceinline__ C ldg_c(const C* p) {
+  return __ldg(p);
+}
+
+// One Stockham stage of radix R over every pencil of the tile:
+// butterfly j reads src[j + r*n/R], twiddles by W_{Ns*R}^{(j mod Ns)*r},
+// and writes dst[(j/Ns)*Ns*R + (j mod Ns) + r*Ns].  The stage twiddle table
+// holds W_{Ns*R}^{p*r} at p*Rp + r, Rp = R rounded up to even.
+template <int R, typename C>
+__device__ __forceinline__ void stage(const C* __restrict__ src, C* __restrict__ dst,
+                                      const C* __restrict__ tw, int n, int Ns, int W, int pitch) {
+  const int nb = n / R;
+  const int total = W * nb;
+  for (int f = threadIdx.x; f < total; f += blockDim.x) {
+    const int c = f / nb;
+    const int j = f - c * nb;
+    const C* s = src + c * pitch;
+    C* o = dst + c * pitch;
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = s[spad(j + r * nb)];
+    const int p = j % Ns;
+    if (Ns > 1) {
+      const C* t = tw + p * (R + (R & 1));
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], ldg_c(t + r));
+    }
+    dft<R>(v);
+    const int base = (j - p) * R + p;
+#pragma unroll
+    for (int r = 0; r < R; ++r) o[spad(base + r * Ns)] = v[r];
+  }
+}
+
+// Runs every stage; returns the buffer holding the natural-order result.
+template <typename C>
+__device__ C* run_stages(const PassDesc& d, C* b0, C* b1) {
+  const C* tw = static_cast<const C*>(d.tw);
+  C* src = b0;
+  C* dst = b1;
+  for (int s = 0; s < d.nstages; ++s) {
+    const StageInfo si = d.st[s];
+    const C* t = tw + si.tw_off;
+    switch (si.radix) {
+      case 16: stage<16>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 8: stage<8>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 4: stage<4>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 2: stage<2>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 3: stage<3>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 5: stage<5>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 7: stage<7>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      default: break;
+    }
+    __syncthreads();
+    C* tmp = src;
+    src = dst;
+    dst = tmp;
+  }
+  return src;
+}
+
+// Transforms tile `tile` of pass `d` (tiles enumerate (batch, column block)).
+// `smem_raw` holds two buffers of d.W * d.pitch elements.  When
+// d.col_in_off / d.col_out_off are set, column c of the tile starts at those
+// element offsets instead of c * cs.
+template <typename T>
+__device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem_raw) {
+  using C = typename CxT<T>::type;
+  C* b0 = reinterpret_cast<C*>(smem_raw);
+  C* b1 = b0 + d.W * d.pitch;
+
+  const int64_t tiles = (d.ncols + d.W - 1) / d.W;
+  const int64_t bq = tile / tiles;
+  const int64_t c0 = (tile - bq * tiles) * d.W;
+  const int64_t b_hi = bq / d.nb_lo;
+  const int64_t b = bq - b_hi * d.nb_lo;
+  const int W = d.W, n = d.n;
+  const C* __restrict__ in = static_cast<const C*>(d.in) + b * d.in_bs + b_hi * d.in_bs2;
+  const uint32_t fl = d.flags;
+  const C* chirp = static_cast<const C*>(d.chirp);
+
+  // ---- load (+ conj, chirp, zero padding) ---------------------------------
+  const int total = W * n;
+  for (int f = threadIdx.x; f < total; f += blockDim.x) {
+    int c, i;
+    if (d.load_cfast) {
+      c = f % W;
+      i = f / W;
+    } else {
+      c = f / n;
+      i = f - c * n;
+    }
+    const int64_t col = c0 + c;
+    C v = cmake<C>(T(0), T(0));
+    bool valid = col < d.ncols;
+    int64_t l = 0;
+    if (fl & (F_PAD_IN | F_CHIRP_IN)) {
+      l = int64_t(i) * d.lin_es + col * d.lin_cs;
+      if ((fl & F_PAD_IN) && l >= d.n_in) valid = false;
+    }
+    if (valid) {
+      const int64_t cb = d.col_in_off ? d.col_in_off[col] : col * d.in_cs;
+      v = in[cb + int64_t(i) * d.in_es];
+      if (fl & F_CONJ_IN) v.y = -v.y;
+      if (fl & F_CHIRP_IN) v = cmul(v, chirp[l]);
+    }
+    b0[c * d.pitch + spad(i)] = v;
+  }
+  __syncthreads();
+
+  C* res = run_stages<C>(d, b0, b1);
+
+  if (fl & F_BLUE) {
+    // spectrum * filter, then the inverse DFT as conj(DFT(conj(.)))
+    const C* filt = static_cast<const C*>(d.filter);
+    for (int f = threadIdx.x; f < total; f += blockDim.x) {
+      const int c = f / n, kk = f - c * n;
+      C* p = res + c * d.pitch + spad(kk);
+      *p = cconj(cmul(*p, filt[kk]));
+    }
+    __syncthreads();
+    C* other = (res == b0) ? b1 : b0;
+    res = run_stages<C>(d, res, other);
+  }
+
+  // ---- store (+ twiddle, filter, chirp, scale, conj, truncation) ---------
+  C* __restrict__ out = static_cast<C*>(d.out) + b * d.out_bs + b_hi * d.out_bs2;
+  const C* tw4_lo = static_cast<const C*>(d.tw4_lo);
+  const C* tw4_hi = static_cast<const C*>(d.tw4_hi);
+  const C* filt = static_cast<const C*>(d.filter);
+  const int64_t tw4_mask = (int64_t(1) << d.tw4_shift) - 1;
+  for (int f = threadIdx.x; f < total; f += blockDim.x) {
+    int c, kk;
+    if (d.store_cfast) {
+      c = f % W;
+      kk = f / W;
+    } else {
+      c = f / n;
+      kk = f - c * n;
+    }
+    const int64_t col = c0 + c;
+    if (col >= d.ncols) continue;
+    int64_t l = int64_t(kk) * d.lout_es + col * d.lout_cs;
+    if ((fl & F_TRUNC_OUT) && l >= d.n_out) continue;
+    C v = res[c * d.pitch + spad(kk)];
+    if (fl & F_TW4) {
+      const int64_t e = (fl & F_TW4_BATCH) ? b : col;
+      const int64_t t = (e * int64_t(kk)) % d.tw4_n;
+      v = cmul(v, cmul(tw4_hi[t >> d.tw4_shift], tw4_lo[t & tw4_mask]));
+    }
+    if (fl & F_FILTER_OUT) v = cconj(cmul(v, filt[l]));
+    if (fl & (F_BLUE | F_CHIRP_OUT)) v = cmul(cconj(v), chirp[l]);
+    if (fl & F_SCALE) v = cscale(v, T(d.scale));
+    if (fl & F_CONJ_OUT) v.y = -v.y;
+    const int64_t cb = d.col_out_off ? d.col_out_off[col] : col * d.out_cs;
+    out[cb + int64_t(kk) * d.out_es] = v;
+  }
+}
+
+
+}  // namespace gbfft

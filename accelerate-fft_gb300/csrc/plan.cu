@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -19,6 +20,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -216,22 +218,56 @@ void Builder::tw4_for(int64_t N, PassSpec& ps) {
 
 // chirp c[l] = exp(-i*pi*(l^2 mod 2n)/n), l < n; filter = DFT_m(b)/m with
 // b[l] = conj(c[|l|]) on the wrapped indices (-n, n).
+void blue_tables(int64_t n, int64_t m, std::vector<cd>& chirp, std::vector<cd>& b) {
+  chirp.assign(static_cast<size_t>(n), cd(0, 0));
+  b.assign(static_cast<size_t>(m), cd(0, 0));
+  for (int64_t l = 0; l < n; ++l) {
+    const int64_t q = int64_t((__int128(l) * l) % (2 * n));
+    chirp[size_t(l)] = unit_root(q, 2 * n);  // exp(-2*pi*i*q/(2n)) = exp(-i*pi*q/n)
+  }
+  for (int64_t l = 0; l < n; ++l) {
+    b[size_t(l)] = std::conj(chirp[size_t(l)]);
+    if (l > 0) b[size_t(m - l)] = std::conj(chirp[size_t(l)]);
+  }
+  host_fft_fp64(b);
+  const double inv = 1.0 / double(m);
+  for (auto& v : b) v *= inv;
+}
+
+void Builder::precompute_blue(const std::vector<std::pair<int64_t, int64_t>>& nm) {
+  std::vector<std::pair<int64_t, int64_t>> todo;
+  for (const auto& k : nm)
+    if (!blue_cache.count(k) && !blue_pre.count(k)) todo.push_back(k);
+  std::sort(todo.begin(), todo.end());
+  todo.erase(std::unique(todo.begin(), todo.end()), todo.end());
+  if (todo.empty()) return;
+  std::vector<std::pair<std::vector<cd>, std::vector<cd>>> res(todo.size());
+  std::atomic<size_t> next{0};
+  unsigned nt = std::max(1u, std::thread::hardware_concurrency());
+  nt = std::min<unsigned>(nt, unsigned(todo.size()));
+  std::vector<std::thread> pool;
+  for (unsigned t = 0; t < nt; ++t)
+    pool.emplace_back([&] {
+      for (size_t i; (i = next.fetch_add(1)) < todo.size();)
+        blue_tables(todo[i].first, todo[i].second, res[i].first, res[i].second);
+    });
+  for (auto& th : pool) th.join();
+  for (size_t i = 0; i < todo.size(); ++i) blue_pre.emplace(todo[i], std::move(res[i]));
+}
+
 void Builder::blue_for(int64_t n, int64_t m, PassSpec& ps) {
   auto key = std::make_pair(n, m);
   auto it = blue_cache.find(key);
   if (it == blue_cache.end()) {
-    std::vector<cd> chirp(static_cast<size_t>(n)), b(size_t(m), cd(0, 0));
-    for (int64_t l = 0; l < n; ++l) {
-      const int64_t q = int64_t((__int128(l) * l) % (2 * n));
-      chirp[size_t(l)] = unit_root(q, 2 * n);  // exp(-2*pi*i*q/(2n)) = exp(-i*pi*q/n)
+    std::vector<cd> chirp, b;
+    auto pre = blue_pre.find(key);
+    if (pre != blue_pre.end()) {
+      chirp.swap(pre->second.first);
+      b.swap(pre->second.second);
+      blue_pre.erase(pre);
+    } else {
+      blue_tables(n, m, chirp, b);
     }
-    for (int64_t l = 0; l < n; ++l) {
-      b[size_t(l)] = std::conj(chirp[size_t(l)]);
-      if (l > 0) b[size_t(m - l)] = std::conj(chirp[size_t(l)]);
-    }
-    host_fft_fp64(b);
-    const double inv = 1.0 / double(m);
-    for (auto& v : b) v *= inv;
     Blue bl;
     bl.chirp = add(chirp);
     bl.filter = add(b);
@@ -283,12 +319,6 @@ static PassSpec blank_pass() {
   return ps;
 }
 
-// ---------------------------------------------------------------------------
-// Axis geometry: element (o, c, i) at o*os + c*cs + i*es, o < outer, c < ncols.
-struct Axis {
-  int64_t n, es, cs, ncols, os, outer;
-};
-
 static int cap_for(bool dbl) { return dbl ? kCapC64 : kCapC32; }
 
 // Split n = n1*n2 (n1 strided first pass, n2 second) with both <= cap,
@@ -315,9 +345,9 @@ static bool split_four_step(int64_t n, int cap, int64_t& n1, int64_t& n2) {
 // Appends the passes of one axis.  `first`: this axis reads the user's
 // input; later axes work on the output buffer.
 int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
-             int64_t& scratch1, int64_t& scratch2, std::string& desc) {
+             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap_in) {
   const bool dbl = B.dbl;
-  const int cap = cap_for(dbl);
+  const int cap = cap_in > 0 ? cap_in : cap_for(dbl);
   const int src = first ? R_IN : R_OUT;
   char buf[256];
   if (ax.n <= 1) return GBFFT_OK;

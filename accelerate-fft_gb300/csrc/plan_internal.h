@@ -46,18 +46,23 @@ struct Builder {
   std::map<int64_t, Tw4> tw4_cache;
   std::map<std::pair<int64_t, int64_t>, Blue> blue_cache;
   std::map<int64_t, size_t> roots_cache;
+  // Bluestein tables computed ahead (in parallel) for (n, m): chirp, filter
+  std::map<std::pair<int64_t, int64_t>, std::pair<std::vector<cd>, std::vector<cd>>> blue_pre;
 
   size_t add(const std::vector<cd>& v);
   bool stages_for(int n, PassSpec& ps);
   void tw4_for(int64_t N, PassSpec& ps);
   void blue_for(int64_t n, int64_t m, PassSpec& ps);
   size_t roots_for(int64_t N);  // table of W_N^t, t < N
+  // compute the Bluestein chirp / filter of every (n, m) on all host cores
+  void precompute_blue(const std::vector<std::pair<int64_t, int64_t>>& nm);
 };
 
 cd unit_root(int64_t t, int64_t L);  // exp(-2*pi*i*t/L), exact reduction
 bool factor_device(int64_t n, std::vector<int>& out);
 bool is_fast_length(int64_t n);
 int64_t bluestein_length(int64_t n);
+void blue_tables(int64_t n, int64_t m, std::vector<cd>& chirp, std::vector<cd>& filter);
 void host_fft_fp64(std::vector<cd>& x);
 void choose_tile(PassSpec& ps, bool dbl);
 bool fault_injected(const char* what);   // GBFFT_FAULT_INJECT=alloc,...
@@ -86,6 +91,12 @@ struct gbfft_plan {
 
 
 namespace gbfft {
+struct Axis {
+  int64_t n, es, cs, ncols, os, outer;  // element (o, c, i) at o*os + c*cs + i*es
+};
+int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
+             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap = 0);
+void* role_ptr(const gbfft_plan* p, int role, const void* in, void* out);
 int build_plan(gbfft_plan* p, bool dry);
 int build_split_plan(gbfft_plan* p);
 int exec_passes(const gbfft_plan* p, const std::vector<PassSpec>& passes, int mode, double inv_norm,

@@ -8,17 +8,6 @@ int build_split_plan(gbfft_plan*) { return GBFFT_ERR_UNSUPPORTED; }
 }  // namespace gbfft
 
 extern "C" {
-int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t, const int64_t*, const int64_t*,
-                             const int*, int) {
-  if (out) *out = nullptr;
-  return GBFFT_ERR_UNSUPPORTED;
-}
-int gbfft_ragged_exec(const gbfft_ragged_plan*, const void*, void*, void*) { return GBFFT_ERR_UNSUPPORTED; }
-int gbfft_ragged_exec_per_transform(const gbfft_ragged_plan*, const void*, void*, void*) {
-  return GBFFT_ERR_UNSUPPORTED;
-}
-int gbfft_ragged_plan_destroy(gbfft_ragged_plan*) { return GBFFT_OK; }
-int gbfft_ragged_status(const gbfft_ragged_plan*, void*) { return GBFFT_ERR_UNSUPPORTED; }
 int gbfft_specconv_plan_create(gbfft_specconv_plan** out, int64_t, int64_t, int64_t, int64_t, int) {
   if (out) *out = nullptr;
   return GBFFT_ERR_UNSUPPORTED;

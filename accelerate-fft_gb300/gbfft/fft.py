@@ -150,3 +150,54 @@ def fft3D(mode, arr, stream=None):
     if arr.dim() != 3:
         raise ValueError("fft3D: rank 3 required")
     return _run(L.KIND_FULL, mode, arr, stream)
+
+
+class RaggedPlan:
+    """Many 1D transforms of uneven lengths and modes over one flat buffer,
+    run by one persistent launch (gbfft_ragged_plan_create / _exec)."""
+
+    def __init__(self, lengths, modes, offsets=None, dtype=torch.complex64):
+        import numpy as np
+        self.lengths = np.ascontiguousarray(np.asarray(lengths, dtype=np.int64))
+        self.modes = np.ascontiguousarray(np.asarray([mode_code(m) for m in modes], dtype=np.int32))
+        self.count = len(self.lengths)
+        if offsets is None:
+            self.offsets = np.concatenate([[0], np.cumsum(self.lengths)[:-1]]).astype(np.int64) \
+                if self.count else np.zeros(0, np.int64)
+            off_arg = None
+        else:
+            self.offsets = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
+            off_arg = self.offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        self.total = int((self.offsets + self.lengths).max()) if self.count else 0
+        self.dtype = dtype
+        h = ctypes.c_void_p()
+        L.check(L.lib().gbfft_ragged_plan_create(
+            ctypes.byref(h), self.count, self.lengths.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            off_arg, self.modes.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+            L.C64 if dtype == torch.complex128 else L.C32), "gbfft_ragged_plan_create")
+        self.handle = h
+
+    def exec_ptr(self, in_ptr, out_ptr, stream=None, per_transform=False):
+        f = L.lib().gbfft_ragged_exec_per_transform if per_transform else L.lib().gbfft_ragged_exec
+        L.check(f(self.handle, ctypes.c_void_p(in_ptr), ctypes.c_void_p(out_ptr), _stream(stream)),
+                "gbfft_ragged_exec")
+
+    def __call__(self, x, out=None, stream=None, per_transform=False):
+        if out is None:
+            out = torch.zeros_like(x)
+        self.exec_ptr(x.data_ptr(), out.data_ptr(), stream, per_transform)
+        return out
+
+    def status(self, stream=None):
+        return L.lib().gbfft_ragged_status(self.handle, _stream(stream))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            L.lib().gbfft_ragged_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

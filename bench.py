@@ -118,6 +118,10 @@ WORKLOADS = {
                            desc="fft innermost, Complex Float 4096x1009 (Bluestein), N(0,1)"),
     "fft1d_1024_c64": dict(kind="full", shape=(1024,), dtype="c64", mode="forward",
                            desc="fft1D Forward, Complex Double N=1024, U[-1,1]"),
+    "ragged_20000": dict(kind="ragged", count=20000, dtype="c32",
+                         desc="ragged batch: 20000 Complex Float transforms, lengths log-uniform in "
+                              "[16, 65536] (70% 7-smooth, 30% prime), Forward/Inverse p=1/2, N(0,1), "
+                              "one persistent launch"),
 }
 
 
@@ -358,6 +362,156 @@ def run_gbfft(args, wl):
         torch.distributed.destroy_process_group()
 
 
+def run_ragged(args, wl):
+    import numpy as np
+    import torch
+
+    import gbfft
+    from gbfft import _lib as L
+    from gbfft import synth
+
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    lengths, modes = synth.ragged_lengths(wl["count"], seed=4)
+    total = int(lengths.sum())
+    g = torch.Generator().manual_seed(1234 + rank)
+    x_cpu = torch.complex(torch.randn(total, generator=g), torch.randn(total, generator=g))
+    x = x_cpu.to(dev)
+    y = torch.empty_like(x)
+    t0 = time.perf_counter()
+    plan = gbfft.RaggedPlan(lengths, modes)
+    plan_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    fl = float(np.sum(5.0 * lengths * np.log2(np.maximum(lengths, 2))))
+    bytes_alg = 2.0 * total * 8
+
+    def timed(per_transform, steps, warm):
+        for _ in range(warm):
+            plan.exec_ptr(x.data_ptr(), y.data_ptr(), stream, per_transform)
+        torch.cuda.synchronize()
+        ts = []
+        for k in range(steps):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            plan.exec_ptr(x.data_ptr(), y.data_ptr(), stream, per_transform)
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return ts
+
+    if world > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    ts = timed(False, args.steps, args.warmup)
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop() if sampler else None
+    ms = sum(ts) / len(ts)
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    status = plan.status()
+    value = fl * world / (ms * 1e-3) / 1e9
+    peak, peak_kind = load_peaks()
+    ach = bytes_alg / (ms * 1e-3) / 1e9
+    per_ms = statistics.mean(timed(True, 3, 1)) if rank == 0 else None
+    # accuracy on a sample of transforms vs FP64
+    rel = None
+    if rank == 0 and not args.no_check:
+        yy = y.cpu().numpy()
+        xx = x_cpu.numpy()
+        rng = np.random.default_rng(0)
+        errs = []
+        for i in rng.choice(len(lengths), 200, replace=False):
+            n, o = int(lengths[i]), int(plan.offsets[i])
+            r = np.fft.fft(xx[o:o + n].astype(np.complex128)) if modes[i] == -1 else \
+                np.fft.ifft(xx[o:o + n].astype(np.complex128))
+            errs.append(float(np.linalg.norm(yy[o:o + n] - r) / np.linalg.norm(r)))
+        rel = max(errs)
+    hx = x_cpu.pin_memory()
+    hy = torch.empty_like(hx).pin_memory()
+    e2e = []
+    for k in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        x.copy_(hx, non_blocking=True)
+        plan.exec_ptr(x.data_ptr(), y.data_ptr(), stream)
+        hy.copy_(y, non_blocking=True)
+        b.record(stream)
+        torch.cuda.synchronize()
+        if k >= 2:
+            e2e.append(a.elapsed_time(b))
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline_ragged(lengths, modes, plan.offsets, x_cpu.numpy())
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": wl["desc"], "count": int(len(lengths)), "elements": total,
+                       "seed": 4, "l2": "flushed (256 MiB write) between timed steps; working set "
+                       "2x%d MiB" % (total * 8 >> 20), "plan_seconds": plan_s,
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                         "frac": ach / peak, "traffic": None, "peak_source": peak_kind,
+                         "kernel": "ragged_kernel<float> (the single persistent launch)",
+                         "bytes_alg_per_launch": bytes_alg, "kernel_ms": ms},
+            "per_transform_comparator": {"ms_per_step": per_ms,
+                                         "value": fl / (per_ms * 1e-3) / 1e9 if per_ms else None,
+                                         "launches_per_step": "one launch sequence per transform"},
+            "rel_err_vs_fp64_max_of_200": rel, "device_status": status,
+            "e2e": {"value": fl * world / (statistics.mean(e2e) * 1e-3) / 1e9, "unit": "GFLOP/s",
+                    "h2d_bytes_per_step": total * 8, "d2h_bytes_per_step": total * 8,
+                    "ms_per_step": statistics.mean(e2e)},
+            "gpu_launches": args.steps, "clocks": clocks, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline_ragged(lengths, modes, offsets, x_np, budget_s=12.0):
+    """The oracle on a bounded prefix of the ragged batch, one transform at a
+    time on all host cores (threads over transforms)."""
+    import concurrent.futures as cf
+    import numpy as np
+    from oracle import lib as O
+    threads = os.cpu_count() or 1
+    x64 = x_np.astype(np.complex64)
+
+    def one(i):
+        n, o = int(lengths[i]), int(offsets[i])
+        O.fft1D(0 if modes[i] == -1 else 2, x64[o:o + n], threads=1)
+        return 5.0 * n * math.log2(max(n, 2))
+
+    done_fl, done_n = 0.0, 0
+    t0 = time.perf_counter()
+    order = np.random.default_rng(0).permutation(len(lengths))
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        for start in range(0, len(order), threads * 4):
+            batch = order[start:start + threads * 4]
+            done_fl += sum(ex.map(one, batch))
+            done_n += len(batch)
+            if time.perf_counter() - t0 > budget_s:
+                break
+    dt = time.perf_counter() - t0
+    return {"value": done_fl / dt / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+            "sample": "%d of the %d transforms (random order), oracle C++ restatement of Adhoc.hs, "
+                      "one transform per host thread" % (done_n, len(lengths))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -375,6 +529,8 @@ def main():
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, wl)
+    elif wl["kind"] == "ragged":
+        run_ragged(args, wl)
     else:
         run_gbfft(args, wl)
 

@@ -1,0 +1,91 @@
+"""GPU tests of the ragged batch (one persistent launch over many transforms
+of uneven lengths and mixed modes) against an FP64 FFT per transform and
+against the one-launch-per-transform comparator."""
+import numpy as np
+import pytest
+import torch
+
+from util import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def ref_segment(x, mode):
+    x = x.astype(np.complex128)
+    if mode == -1:
+        return np.fft.fft(x)
+    y = np.fft.ifft(x)
+    return y * len(x) if mode == 1 else y
+
+
+def check_segments(lengths, modes, offsets, x, y, tol=4e-6, sample=None):
+    idx = range(len(lengths)) if sample is None else sample
+    for i in idx:
+        n, o = int(lengths[i]), int(offsets[i])
+        if n == 0:
+            continue
+        e = rel_l2(y[o:o + n], ref_segment(x[o:o + n], int(modes[i])))
+        assert e < tol, (i, n, int(modes[i]), e)
+
+
+def test_ragged_small_mixed(gbfft_lib):
+    g = gbfft_lib
+    from gbfft import synth
+    lengths, modes = synth.ragged_lengths(300, seed=11, hi=20000)
+    extra = np.array([1, 2, 3, 5, 7, 16, 17, 97, 4096, 4097, 8192, 8191, 12289, 65536, 65521], np.int64)
+    lengths = np.concatenate([lengths, extra])
+    modes = np.concatenate([modes, np.array([-1, 1, 2] * 5, np.int32)])
+    rng = np.random.default_rng(0)
+    total = int(lengths.sum())
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    plan = g.RaggedPlan(lengths, modes)
+    xt = torch.from_numpy(x).cuda()
+    y = plan(xt)
+    torch.cuda.synchronize()
+    assert plan.status() == 0
+    yn = y.cpu().numpy()
+    check_segments(lengths, modes, plan.offsets, x, yn)
+    # relaunch with fresh buffers (graph parameter update) and the comparator
+    y2 = torch.empty_like(xt)
+    plan(xt, out=y2)
+    y3 = plan(xt, per_transform=True)
+    torch.cuda.synchronize()
+    assert torch.equal(y2, y)
+    assert rel_l2(y3.cpu().numpy(), yn) < 4e-6
+    assert torch.equal(xt.cpu(), torch.from_numpy(x))
+
+
+def test_ragged_offsets_with_gaps_and_double(gbfft_lib):
+    g = gbfft_lib
+    lengths = np.array([16, 1000, 1009, 5, 8192, 3], np.int64)
+    modes = np.array([-1, 2, 1, -1, 2, 1], np.int32)
+    offsets = np.array([0, 40, 1100, 3000, 3020, 12000], np.int64)
+    total = 12010
+    rng = np.random.default_rng(1)
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex128)
+    plan = g.RaggedPlan(lengths, modes, offsets=offsets, dtype=torch.complex128)
+    y = plan(torch.from_numpy(x).cuda()).cpu().numpy()
+    check_segments(lengths, modes, offsets, x, y, tol=1e-12)
+    # gaps are left untouched (zeros from zeros_like)
+    assert np.all(y[20:40] == 0)
+
+
+def test_ragged_config4_full_size(gbfft_lib):
+    # 20,000 transforms, lengths 16..65536 (70% 7-smooth, 30% prime), mixed modes
+    g = gbfft_lib
+    from gbfft import synth
+    lengths, modes = synth.ragged_lengths(20000, seed=4)
+    total = int(lengths.sum())
+    gen = torch.Generator().manual_seed(4)
+    x = torch.complex(torch.randn(total, generator=gen), torch.randn(total, generator=gen))
+    plan = g.RaggedPlan(lengths, modes)
+    xt = x.cuda()
+    y = plan(xt)
+    yp = plan(xt, per_transform=True)
+    torch.cuda.synchronize()
+    assert plan.status() == 0
+    yn = y.cpu().numpy()
+    assert rel_l2(yn, yp.cpu().numpy()) < 4e-6
+    rng = np.random.default_rng(4)
+    sample = rng.choice(len(lengths), 300, replace=False)
+    check_segments(lengths, modes, plan.offsets, x.numpy(), yn, sample=sample)
