@@ -714,6 +714,7 @@ const char* gbfft_error_string(int status) {
     case GBFFT_ERR_NULL_PLAN: return "null plan";
     case GBFFT_ERR_TIMEOUT: return "bounded device wait timed out";
     case GBFFT_ERR_INTERNAL: return "internal error";
+    case GBFFT_ERR_TOO_LARGE: return "request exceeds the fixed work area of gbfft_fft_noalloc";
   }
   return "unknown status";
 }

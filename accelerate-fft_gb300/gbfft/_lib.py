@@ -17,6 +17,7 @@ ERR_CUDA = 4
 ERR_NULL_PLAN = 5
 ERR_TIMEOUT = 6
 ERR_INTERNAL = 7
+ERR_TOO_LARGE = 8
 
 FORWARD, REVERSE, INVERSE = -1, 1, 2
 C32, C64 = 0, 1
@@ -54,6 +55,7 @@ SIGNATURES = {
     "gbfft_specconv_fwd": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "gbfft_specconv_bwd": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbfft_specconv_plan_destroy": (_i, [_vp]),
+    "gbfft_fft_noalloc": (_i, [_i, _i64, _i64, _i, _vp, _vp, _vp]),
 }
 
 _lib = None

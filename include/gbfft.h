@@ -35,7 +35,8 @@ enum {
   GBFFT_ERR_CUDA = 4,         /* a CUDA runtime call failed                      */
   GBFFT_ERR_NULL_PLAN = 5,
   GBFFT_ERR_TIMEOUT = 6,      /* a bounded device wait gave up (ragged executor) */
-  GBFFT_ERR_INTERNAL = 7
+  GBFFT_ERR_INTERNAL = 7,
+  GBFFT_ERR_TOO_LARGE = 8     /* request exceeds gbfft_fft_noalloc's fixed work area */
 };
 
 /* ---- Mode: src/Data/Array/Accelerate/Math/FFT/Mode.hs:15-26 -------------
@@ -161,6 +162,22 @@ int gbfft_specconv_fwd(const gbfft_specconv_plan* plan, const void* d_x, const v
 int gbfft_specconv_bwd(const gbfft_specconv_plan* plan, const void* d_x, const void* d_H,
                        const void* d_gy, void* d_gx, void* d_gH, void* stream);
 int gbfft_specconv_plan_destroy(gbfft_specconv_plan* plan);
+
+/* ---- allocation-free transform ------------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory -- a host that owns the device heap (Accelerate's
+ * PTX backend passes arrays from its own allocator) or code recording a CUDA
+ * graph by stream capture, where cudaMalloc is not allowed.  Transforms
+ * `batch` contiguous rows of length n (Bluestein's algorithm, four passes,
+ * any n) with Mode semantics as gbfft_exec (Inverse divides by n), reading
+ * d_in and writing d_out, and allocates nothing: its tables and padded work
+ * sequences live in one fixed 16 MiB __device__ array per device, kept until
+ * the process exits.  The first call on a device sets that array up (make it
+ * before any stream capture).  Calls share the array, so calls that overlap
+ * on the GPU race.  Requests whose tables plus 2 * batch * m elements (m, the
+ * padded length, is about 2n to 4n) exceed 16 MiB return GBFFT_ERR_TOO_LARGE. */
+int gbfft_fft_noalloc(int mode, int64_t n, int64_t batch, int dtype, const void* d_in, void* d_out,
+                      void* stream);
 
 #ifdef __cplusplus
 }
