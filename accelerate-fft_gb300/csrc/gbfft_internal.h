@@ -32,6 +32,7 @@ enum PassFlags : uint32_t {
   F_FILTER_OUT = 1u << 8,  // multiply by filter[l] then conjugate, on store
   F_CHIRP_OUT = 1u << 9,   // conjugate then multiply by chirp[l] on store
   F_TRUNC_OUT = 1u << 10,  // store only logical output index l < n_out
+  F_SPEC = 1u << 11,       // in-kernel spectral multiply: DFT, * filter[l], conj, DFT
 };
 
 // Kernel families a pass can run on.

@@ -122,6 +122,28 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
 
   C* res = run_stages<C>(d, b0, b1);
 
+  if (fl & F_SPEC) {
+    // spectrum * filter[k*lout_es + col*lout_cs], then the next transform of
+    // the conjugate (the first axis of an inverse taken as conj(DFT(conj)))
+    const C* filt = static_cast<const C*>(d.filter);
+    for (int f = threadIdx.x; f < total; f += blockDim.x) {
+      int c, kk;
+      if (d.store_cfast) {
+        c = f % W;
+        kk = f / W;
+      } else {
+        c = f / n;
+        kk = f - c * n;
+      }
+      const int64_t col = c0 + c;
+      C* p = res + c * d.pitch + spad(kk);
+      const C h = (col < d.ncols) ? filt[int64_t(kk) * d.lout_es + col * d.lout_cs] : cmake<C>(T(0), T(0));
+      *p = cconj(cmul(*p, h));
+    }
+    __syncthreads();
+    C* other = (res == b0) ? b1 : b0;
+    res = run_stages<C>(d, res, other);
+  }
   if (fl & F_BLUE) {
     // spectrum * filter, then the inverse DFT as conj(DFT(conj(.)))
     const C* filt = static_cast<const C*>(d.filter);

@@ -201,3 +201,54 @@ class RaggedPlan:
             self.close()
         except Exception:
             pass
+
+
+class SpecConvPlan:
+    """Spectral convolution y_b = fft3D Inverse (fft3D Forward (x_b) * H) over a
+    batch of d x h x w fields, with its adjoint (gbfft_specconv_*)."""
+
+    def __init__(self, batch, d, h, w, dtype=torch.complex64):
+        self.shape = (int(batch), int(d), int(h), int(w))
+        self.dtype = dtype
+        hd = ctypes.c_void_p()
+        L.check(L.lib().gbfft_specconv_plan_create(ctypes.byref(hd), *self.shape,
+                                                   L.C64 if dtype == torch.complex128 else L.C32),
+                "gbfft_specconv_plan_create")
+        self.handle = hd
+
+    def _check(self, t, shape):
+        if not t.is_cuda or not t.is_contiguous() or tuple(t.shape) != shape or t.dtype != self.dtype:
+            raise ValueError("gbfft specconv: expected contiguous %s CUDA tensor of shape %s"
+                             % (self.dtype, shape))
+
+    def forward(self, x, H, out=None, stream=None):
+        self._check(x, self.shape)
+        self._check(H, self.shape[1:])
+        y = torch.empty_like(x) if out is None else out
+        L.check(L.lib().gbfft_specconv_fwd(self.handle, ctypes.c_void_p(x.data_ptr()),
+                                           ctypes.c_void_p(H.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                           _stream(stream)), "gbfft_specconv_fwd")
+        return y
+
+    def backward(self, x, H, gy, stream=None):
+        self._check(x, self.shape)
+        self._check(H, self.shape[1:])
+        self._check(gy, self.shape)
+        gx = torch.empty_like(x)
+        gH = torch.empty_like(H)
+        L.check(L.lib().gbfft_specconv_bwd(self.handle, ctypes.c_void_p(x.data_ptr()),
+                                           ctypes.c_void_p(H.data_ptr()), ctypes.c_void_p(gy.data_ptr()),
+                                           ctypes.c_void_p(gx.data_ptr()), ctypes.c_void_p(gH.data_ptr()),
+                                           _stream(stream)), "gbfft_specconv_bwd")
+        return gx, gH
+
+    def close(self):
+        if getattr(self, "handle", None):
+            L.lib().gbfft_specconv_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
