@@ -40,6 +40,7 @@ enum KernelId : int {
   K_PENCIL = 0,   // generic shared-memory pencil kernel (any length <= cap, fused ops)
   K_ROW = 1,      // register-resident contiguous-row kernel (specialised lengths)
   K_COL4096 = 2,  // 8-CTA cluster kernel for stride-S axes of length 4096
+  K_ROW_TC = 3,   // contiguous rows, radix-16 stages as split-FP16 tensor-core GEMMs
 };
 
 struct StageInfo {
@@ -85,6 +86,7 @@ struct PassDesc {
   const void* tw4_lo;
   const void* tw4_hi;
   int src_role, dst_role;      // buffer roles (ragged executor)
+  const void* tcmat;           // K_ROW_TC: D_hi, D_lo (32 x 32 f16 each, N x K row-major)
   const int64_t* col_in_off;   // optional per-column element offsets (ragged groups)
   const int64_t* col_out_off;
   const void* chirp;   // Bluestein chirp c[l] = exp(-i*pi*l^2/n), l < n
@@ -104,6 +106,9 @@ bool row_kernel_available(int n, bool dbl);
 cudaError_t prepare_row_kernels();
 cudaError_t launch_row(const PassDesc& d, bool dbl, cudaStream_t s);
 cudaError_t prepare_col_kernels();
+bool row_tc_available(int n);
+cudaError_t prepare_row_tc_kernels();
+cudaError_t launch_row_tc(const PassDesc& d, cudaStream_t s);
 cudaError_t launch_col4096(const PassDesc& d, bool dbl, cudaStream_t s);
 int col_tile_width(int variant);
 

@@ -7,6 +7,7 @@
 //   setStream + execC2C/execZ2Z .......... PTX.hs:112-124
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -661,6 +662,42 @@ int build_plan(gbfft_plan* p, bool dry) {
   return GBFFT_OK;
 }
 
+// Split-FP16 plans: the FP32 plan with every contiguous-row pass whose
+// length has radix-16 stages moved to the tensor-core kernel.  D is the
+// 32 x 32 real form of the forward DFT-16 (rows: Re y_n then Im y_n;
+// columns: Re x_k then Im x_k), split as D_hi + D_lo in FP16.
+int build_split_plan(gbfft_plan* p) {
+  if (p->dbl) return GBFFT_ERR_INVALID_ARG;
+  int st = build_plan(p, false);
+  if (st != GBFFT_OK) return st;
+  std::vector<__half> dm(2048);
+  for (int n = 0; n < 32; ++n)
+    for (int k = 0; k < 32; ++k) {
+      const int nn = n & 15, kk = k & 15;
+      const cd w = unit_root(int64_t(nn) * kk, 16);  // cos - i sin
+      const double c = w.real(), sn = -w.imag();
+      const double v = (n < 16) ? (k < 16 ? c : sn) : (k < 16 ? -sn : c);
+      const __half h = __float2half_rn(float(v));
+      dm[size_t(n * 32 + k)] = h;
+      dm[size_t(1024 + n * 32 + k)] = __float2half_rn(float(v - double(__half2float(h))));
+    }
+  bool any = false;
+  for (PassSpec& ps : p->passes)
+    if (ps.d.kernel == K_ROW && row_tc_available(ps.d.n)) any = true;
+  if (!any) return GBFFT_OK;  // no radix-16 row pass: the plain kernels serve the plan
+  if (fault_injected("alloc")) return GBFFT_ERR_ALLOC;
+  if (cudaMalloc(&p->d_tcmat, dm.size() * sizeof(__half)) != cudaSuccess) return GBFFT_ERR_ALLOC;
+  if (cudaMemcpy(p->d_tcmat, dm.data(), dm.size() * sizeof(__half), cudaMemcpyHostToDevice) != cudaSuccess)
+    return GBFFT_ERR_CUDA;
+  for (PassSpec& ps : p->passes)
+    if (ps.d.kernel == K_ROW && row_tc_available(ps.d.n)) {
+      ps.d.kernel = K_ROW_TC;
+      ps.d.tcmat = p->d_tcmat;
+    }
+  p->desc += " split-fp16(tensor-core radix-16 rows)";
+  return GBFFT_OK;
+}
+
 void* role_ptr(const gbfft_plan* p, int role, const void* in, void* out) {
   switch (role) {
     case R_IN: return const_cast<void*>(in);
@@ -796,6 +833,7 @@ int gbfft_plan_destroy(gbfft_plan* plan) {
   if (!plan) return GBFFT_OK;
   if (plan->d_tables) cudaFree(plan->d_tables);
   if (plan->d_scratch) cudaFree(plan->d_scratch);
+  if (plan->d_tcmat) cudaFree(plan->d_tcmat);
   delete plan;
   return GBFFT_OK;
 }

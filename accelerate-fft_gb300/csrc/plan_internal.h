@@ -86,6 +86,7 @@ struct gbfft_plan {
   size_t scratch_bytes = 0;
   size_t s2_off = 0;
   int* d_status = nullptr;  // device status word inside d_tables
+  void* d_tcmat = nullptr;  // split-FP16 plans: D_hi, D_lo of the DFT-16 (4 KiB)
   std::string desc;
 };
 

@@ -20,6 +20,8 @@
 //    streams in while the current one is transformed.  Waits are bounded: on
 //    timeout the kernel records GBFFT_ERR_TIMEOUT in the plan's status word
 //    and stops.
+#include <cuda_fp16.h>
+
 #include <algorithm>
 
 #include "butterflies.cuh"
@@ -397,6 +399,275 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_tma_kernel(const Pa
   }
 }
 
+// ---- split-FP16 tensor-core variant (Complex Float) --------------------------
+// Every radix-16 stage runs as a GEMM on the 5th-generation tensor cores:
+// the 128 butterflies of a warpgroup form the rows of A (128 x 32: real then
+// imaginary parts of the 16 inputs), D is the 32 x 32 real form of the
+// forward DFT-16, and Y^T = A * D^T is accumulated in FP32 in tensor memory
+// (tcgen05.mma kind::f16, M = 128, N = 32, K = 32).  Inputs are split as
+// x*s = hi + lo in FP16 with a per-butterfly power-of-two scale s (rows are
+// independent, so the scale is exact to undo) and D = D_hi + D_lo; three
+// products hi*hi + hi*lo + lo*hi recover FP32 accuracy.  TMEM lane r of the
+// accumulator is row r, which is the butterfly of thread r of the warpgroup,
+// so tcgen05.ld 32x32b returns every thread its own 32 outputs.  Twiddles
+// and the radix-8/4/2 stages stay in FP32 on the CUDA cores.
+__device__ __forceinline__ int cm_off(int m, int k) {  // no-swizzle K-major core matrices
+  return (m >> 3) * 512 + (k >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2;
+}
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+  // start address, leading byte offset 128 (K), stride byte offset 512 (M/N),
+  // descriptor version 1, no swizzle
+  return uint64_t((saddr >> 4) & 0x3FFF) | (uint64_t(128 >> 4) << 16) | (uint64_t(512 >> 4) << 32) |
+         (uint64_t(1) << 46);
+}
+constexpr uint32_t kTcIdesc = (1u << 4) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+
+struct TcCtx {
+  unsigned char* a_hi;  // 8 KiB, this warpgroup's A (hi)
+  unsigned char* a_lo;  // 8 KiB (lo)
+  uint32_t b_hi, b_lo;  // shared addresses of D_hi, D_lo (2 KiB each)
+  uint64_t* mbar;
+  uint32_t phase;
+  uint32_t taddr;  // this warpgroup's accumulator columns, lane 0
+  int row;         // thread's row in the warpgroup (0..127)
+  int wg;          // warpgroup index in the CTA
+  int* status;
+};
+
+__device__ __forceinline__ void tc_dft16(float2 (&v)[16], TcCtx& c) {
+  // per-butterfly power-of-two scale: max |x*s| in [2^13, 2^14)
+  float mx = 0.f;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) mx = fmaxf(mx, fmaxf(fabsf(v[k].x), fabsf(v[k].y)));
+  const int ex = mx > 0.f ? ((__float_as_int(mx) >> 23) & 0xFF) - 127 : 0;
+  const int sh = max(-100, min(100, 13 - ex));
+  const float s = ldexpf(1.f, sh), inv = ldexpf(1.f, -sh);
+#pragma unroll
+  for (int kc = 0; kc < 4; ++kc) {
+    __align__(16) __half hi[8], lo[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = kc * 8 + q;
+      const float x = (k < 16 ? v[k].x : v[k - 16].y) * s;
+      const __half h = __float2half_rn(x);
+      hi[q] = h;
+      lo[q] = __float2half_rn(x - __half2float(h));
+    }
+    *reinterpret_cast<uint4*>(c.a_hi + cm_off(c.row, kc * 8)) = *reinterpret_cast<const uint4*>(hi);
+    *reinterpret_cast<uint4*>(c.a_lo + cm_off(c.row, kc * 8)) = *reinterpret_cast<const uint4*>(lo);
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("bar.sync %0, 128;" ::"r"(1 + c.wg) : "memory");
+  if (c.row == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t ahi = smem_u32(c.a_hi), alo = smem_u32(c.a_lo);
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+      const uint64_t dah = umma_desc(ahi + ks * 256), dal = umma_desc(alo + ks * 256);
+      const uint64_t dbh = umma_desc(c.b_hi + ks * 256), dbl = umma_desc(c.b_lo + ks * 256);
+      const uint32_t acc0 = ks > 0 ? 1u : 0u;
+      asm volatile(
+          "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+          " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(c.taddr),
+          "l"(dah), "l"(dbh), "r"(kTcIdesc), "r"(acc0)
+          : "memory");
+      asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;\n" ::"r"(c.taddr), "l"(dah),
+                   "l"(dbl), "r"(kTcIdesc)
+                   : "memory");
+      asm volatile("tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, 1;\n" ::"r"(c.taddr), "l"(dal),
+                   "l"(dbh), "r"(kTcIdesc)
+                   : "memory");
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(c.mbar))
+                 : "memory");
+  }
+  if (!mbar_wait_bounded(c.mbar, c.phase, c.status)) {
+    // the product never completed: leave the inputs in place (the status
+    // word records the timeout) rather than read an unfinished accumulator
+    c.phase ^= 1u;
+    return;
+  }
+  c.phase ^= 1u;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  uint32_t r[32];
+  const uint32_t lane_base = uint32_t((c.row >> 5) * 32) << 16;
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+        "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+        "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+        "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(c.taddr + lane_base)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = make_float2(__uint_as_float(r[k]) * inv, __uint_as_float(r[k + 16]) * inv);
+}
+
+template <int N, int E, int NS, int R>
+__device__ __forceinline__ void row_compute_tc(float2 (&v)[E], const float2* __restrict__ tw, int t,
+                                               TcCtx& c) {
+  if constexpr (R == 16 && E == 16) {
+    if constexpr (NS > 1) {
+      const int p = t % NS;
+      float2 w[17];
+      derive_tw<16>(w, tw + p * 16);
+#pragma unroll
+      for (int r = 1; r < 16; ++r) v[r] = cmul(v[r], w[r]);
+    }
+    tc_dft16(v, c);
+  } else {
+    row_compute<N, E, NS, R>(v, tw, t);
+  }
+}
+
+template <int N, int E, int NS, int OFF, int R, int... Rest>
+__device__ __forceinline__ void row_stages_tc(float2 (&v)[E], float2* b, const float2* __restrict__ tw,
+                                              int t, TcCtx& c, RL<R, Rest...>) {
+  row_compute_tc<N, E, NS, R>(v, tw + OFF, t, c);
+  if constexpr (sizeof...(Rest) > 0) {
+    row_write<N, E, NS, R>(v, b, t);
+    __syncthreads();
+    constexpr int R2 = rl_first(RL<Rest...>{});
+    row_read<N, E, R2>(v, b, t);
+    __syncthreads();
+    row_stages_tc<N, E, NS * R, OFF + NS * even_up<R>()>(v, b, tw, t, c, RL<Rest...>{});
+  }
+}
+
+template <int N, int ROWS, int... Rs>
+__global__ void __launch_bounds__(ROWS*(N / 16), 1) rowfft_tc_kernel(const PassDesc d) {
+  using C = float2;
+  constexpr int E = 16;
+  constexpr int TH = N / E;
+  constexpr int NT = ROWS * TH;
+  constexpr int NWG = NT / 128;
+  static_assert(NT % 128 == 0, "whole warpgroups");
+  constexpr int R0 = rl_first(RL<Rs...>{});
+  constexpr int RZ = rl_last(RL<Rs...>{});
+  constexpr uint32_t kCols = (32 * NWG <= 32) ? 32 : (32 * NWG <= 64) ? 64 : (32 * NWG <= 128) ? 128 : 256;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t mbar[NWG];
+  __shared__ uint32_t tslot;
+  // layout: [A hi|lo per warpgroup: 16 KiB each][D hi|lo: 4 KiB][exchange: ROWS * N]
+  unsigned char* amem = smem_raw;
+  unsigned char* bmem = smem_raw + NWG * 16384;
+  C* xbuf = reinterpret_cast<C*>(bmem + 4096);
+  const int slot = threadIdx.x / TH;
+  const int t = threadIdx.x - slot * TH;
+  C* b = xbuf + slot * N;
+  const int wg = threadIdx.x >> 7;
+
+  // D_hi / D_lo (32 x 32 f16 each, row-major N x K in global) -> core-matrix layout
+  const __half* dm = static_cast<const __half*>(d.tcmat);
+  for (int i = threadIdx.x; i < 2 * 1024; i += blockDim.x) {
+    const int which = i >> 10, n = (i >> 5) & 31, k = i & 31;
+    *reinterpret_cast<__half*>(bmem + which * 2048 + cm_off(n, k)) = dm[i];
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (threadIdx.x == 0) {
+    for (int g = 0; g < NWG; ++g) mbar_init(&mbar[g], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tslot)),
+                 "r"(kCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+  TcCtx c;
+  c.a_hi = amem + wg * 16384;
+  c.a_lo = c.a_hi + 8192;
+  c.b_hi = smem_u32(bmem);
+  c.b_lo = smem_u32(bmem + 2048);
+  c.mbar = &mbar[wg];
+  c.phase = 0;
+  c.taddr = tslot + uint32_t(32 * wg);
+  c.row = threadIdx.x & 127;
+  c.wg = wg;
+  c.status = d.status;
+
+  const int64_t rows = d.ncols;
+  const int64_t nchunks = (rows + ROWS - 1) / ROWS;
+  const uint32_t fl = d.flags;
+  const float s = float(d.scale);
+  const C* __restrict__ tw = static_cast<const C*>(d.tw);
+  for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    const int64_t row = ch * ROWS + slot;
+    const bool ok = row < rows;
+    const C* __restrict__ in = static_cast<const C*>(d.in) + row * d.in_cs;
+    C v[E];
+#pragma unroll
+    for (int q = 0; q < E / R0; ++q)
+#pragma unroll
+      for (int r = 0; r < R0; ++r) {
+        C x = make_float2(0.f, 0.f);
+        if (ok) x = in[t + TH * (q + r * (E / R0))];
+        if (fl & F_CONJ_IN) x.y = -x.y;
+        v[q * R0 + r] = x;
+      }
+    row_stages_tc<N, E, 1, 0>(v, b, tw, t, c, RL<Rs...>{});
+    if (ok) {
+      C* __restrict__ out = static_cast<C*>(d.out) + row * d.out_cs;
+#pragma unroll
+      for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+        for (int r = 0; r < RZ; ++r) {
+          C x = v[q * RZ + r];
+          if (fl & F_SCALE) x = cscale(x, s);
+          if (fl & F_CONJ_OUT) x.y = -x.y;
+          out[t + TH * (q + r * (E / RZ))] = x;
+        }
+    }
+    __syncthreads();  // the exchange buffer is reused by the next chunk
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (threadIdx.x < 32)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tslot), "r"(kCols) : "memory");
+}
+
+template <int N, int ROWS, int... Rs>
+struct RowTcCfg {
+  static constexpr int threads = ROWS * (N / 16);
+  static size_t smem() { return size_t(threads / 128) * 16384 + 4096 + size_t(ROWS) * N * 8; }
+  static int ctas_per_sm;
+  static cudaError_t prepare() {
+    cudaError_t e = cudaFuncSetAttribute(rowfft_tc_kernel<N, ROWS, Rs...>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem()));
+    if (e != cudaSuccess) return e;
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rowfft_tc_kernel<N, ROWS, Rs...>, threads, smem());
+    ctas_per_sm = nb > 0 ? nb : 1;
+    return e;
+  }
+  static cudaError_t launch(const PassDesc& d, cudaStream_t s, int sms) {
+    const int64_t chunks = (d.ncols + ROWS - 1) / ROWS;
+    const int64_t grid = std::min<int64_t>(chunks, int64_t(sms) * ctas_per_sm);
+    rowfft_tc_kernel<N, ROWS, Rs...><<<unsigned(grid), threads, smem(), s>>>(d);
+    return cudaGetLastError();
+  }
+};
+template <int N, int ROWS, int... Rs>
+int RowTcCfg<N, ROWS, Rs...>::ctas_per_sm = 1;
+
+// lengths with radix-16 stages and whole warpgroups per CTA
+#define GBFFT_ROWTC_TABLE(X)  \
+  X(256, 8, 16, 16)           \
+  X(512, 4, 16, 16, 2)        \
+  X(1024, 2, 16, 16, 4)       \
+  X(2048, 1, 16, 16, 8)       \
+  X(4096, 1, 16, 16, 16)      \
+  X(8192, 1, 16, 16, 16, 2)
+
 template <typename T, int N, int E, int ROWS, int MINB, int... Rs>
 struct RowCfg {
   static constexpr int threads = ROWS * (N / E);
@@ -482,6 +753,32 @@ cudaError_t prepare_row_kernels() {
   GBFFT_ROW_TABLE(X)
 #undef X
   return e;
+}
+
+bool row_tc_available(int n) {
+#define X(N, ROWS, ...) \
+  if (n == N) return true;
+  GBFFT_ROWTC_TABLE(X)
+#undef X
+  return false;
+}
+
+cudaError_t prepare_row_tc_kernels() {
+  cudaError_t e = cudaSuccess;
+#define X(N, ROWS, ...) \
+  if (e == cudaSuccess) e = RowTcCfg<N, ROWS, __VA_ARGS__>::prepare();
+  GBFFT_ROWTC_TABLE(X)
+#undef X
+  return e;
+}
+
+cudaError_t launch_row_tc(const PassDesc& d, cudaStream_t s) {
+  const int sms = g_sms > 0 ? g_sms : 1;
+#define X(N, ROWS, ...) \
+  if (d.n == N) return RowTcCfg<N, ROWS, __VA_ARGS__>::launch(d, s, sms);
+  GBFFT_ROWTC_TABLE(X)
+#undef X
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_row(const PassDesc& d, bool dbl, cudaStream_t s) {

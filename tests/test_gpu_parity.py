@@ -327,3 +327,32 @@ def test_row_kernel_input_not_16_byte_aligned(gbfft_lib):
     plan.exec_ptr("forward", view.data_ptr(), out.data_ptr())
     ref = np.fft.fft(view.cpu().numpy().astype(np.complex128), axis=-1)
     assert rel_l2(out.cpu().numpy(), ref) < 2e-6
+
+
+# ---- split-FP16 tensor-core radix-16 stages ---------------------------------
+@pytest.mark.parametrize("shape,kind", [((4096, 4096), "full"), ((300, 4096), "many"), ((100, 1024), "many"),
+                                        ((64, 256), "many"), ((8, 8192), "many"), ((17, 2048), "many"),
+                                        ((5, 512), "many"), ((3, 256, 256), "full"), ((6, 1000), "many")])
+def test_split_fp16_accuracy(gbfft_lib, shape, kind):
+    # the specification's bar: <= 2e-6 relative L2 against FP64
+    g = gbfft_lib
+    rng = np.random.default_rng(sum(shape))
+    x = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    plan = g.Plan(shape, kind=kind, dtype=torch.complex64, precision="split_fp16")
+    xt = torch.from_numpy(x).cuda()
+    fam = {2: "fft2D", 3: "fft3D"}[len(shape)] if kind == "full" else "fft"
+    for mode in MODES:
+        y = plan(mode, xt).cpu().numpy()
+        e = rel_l2(y, np_reference(fam, MODE_IDX[mode], x))
+        assert e < 2e-6, (shape, kind, mode, e, plan.describe())
+    from gbfft import _lib as L
+    assert L.lib().gbfft_exec_status(plan.handle, None) == 0
+    # zero input stays zero, large and tiny magnitudes keep relative accuracy
+    for scale in (0.0, 1e-20, 1e20):
+        xs = (x * np.float32(scale)).astype(np.complex64)
+        y = plan("forward", torch.from_numpy(xs).cuda()).cpu().numpy()
+        ref = np_reference(fam, 0, xs)
+        if scale == 0.0:
+            assert np.all(y == 0)
+        else:
+            assert rel_l2(y, ref) < 2e-6, scale
