@@ -212,6 +212,297 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(64 * W / U, MINB)
   }
 }
 
+// Push variant: phase-1 results go straight into the owning CTA's receive
+// buffer with st.async (distributed shared memory, completing on the
+// receiver's mbarrier transaction count), so phase 2 reads only local shared
+// memory.  One cluster barrier at the start (before any data is pending)
+// makes every receiver's mbarrier initialisation visible; no barrier is
+// needed between the phases.  Layout: work buffer 8 x GP (phase-1 exchange
+// and phase-2 exchange), receive buffer [b][Kl][x] of 64 * 8 * W elements.
+__device__ __forceinline__ void st_async(uint32_t addr, float2 v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(addr),
+               "f"(v.x), "f"(v.y), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void st_async(uint32_t addr, double2 v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f64 [%0], {%1, %2}, [%3];" ::"r"(addr),
+               "d"(v.x), "d"(v.y), "r"(bar)
+               : "memory");
+}
+constexpr uint32_t kColWaitLimit = 1u << 22;
+
+template <typename T, int W, int U, int MINB>
+__global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(64 * W / U, MINB)
+    colfft4096_push_kernel(const PassDesc d) {
+  using C = typename CxT<T>::type;
+  constexpr int GP = col_gp<W>();
+  constexpr int HS = 8 / U;
+  constexpr uint32_t kRecvBytes = 64u * 8u * W * sizeof(C);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sm = reinterpret_cast<C*>(smem_raw);
+  C* rv = sm + 8 * GP;  // receive buffer
+  __shared__ __align__(8) uint64_t rbar;
+  const int r = int(cg::this_cluster().block_rank());
+  const int64_t tile = int64_t(blockIdx.x) >> 3;
+  const int64_t tpb = d.ncols / W;
+  const int64_t bo = tile / tpb;
+  const int64_t x0 = (tile - bo * tpb) * W;
+  const C* __restrict__ in = static_cast<const C*>(d.in) + bo * d.in_bs + x0;
+  C* __restrict__ out = static_cast<C*>(d.out) + bo * d.out_bs + x0;
+  const C* __restrict__ w = static_cast<const C*>(d.tw);
+  const int64_t ies = d.in_es, oes = d.out_es;
+  const uint32_t fl = d.flags;
+  const int tid = threadIdx.x;
+  const int x = tid % W;
+  const int g = (tid / W) & 7;
+  const int h = tid / (8 * W);
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&rbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // every receiver's mbarrier is initialised before anyone pushes to it;
+  // the wait is deferred until the first push
+  cluster_arrive_release();
+
+  C v[U][8];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int a2 = h + HS * u;
+#pragma unroll
+    for (int a1 = 0; a1 < 8; ++a1) {
+      const int y = 64 * (8 * a1 + a2) + 8 * r + g;
+      C e = in[int64_t(y) * ies + x];
+      if (fl & F_CONJ_IN) e.y = -e.y;
+      v[u][a1] = e;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int a2 = h + HS * u;
+    dft8(v[u]);
+    apply_powers8(v[u], w, 64 * a2);
+#pragma unroll
+    for (int k1 = 0; k1 < 8; ++k1) sm[g * GP + (a2 * 8 + k1) * W + x] = v[u][k1];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int k1 = h + HS * u;
+#pragma unroll
+    for (int a2 = 0; a2 < 8; ++a2) v[u][a2] = sm[g * GP + (a2 * 8 + k1) * W + x];
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&rbar)),
+                 "r"(kRecvBytes)
+                 : "memory");
+  }
+  cluster_wait_acquire();
+  const int b = 8 * r + g;
+  const uint32_t rv0 = smem_u32(rv), bar0 = smem_u32(&rbar);
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int k1 = h + HS * u;
+    dft8(v[u]);
+    apply_powers8(v[u], w, 8 * b, tw_at(w, b * k1));
+    // K = k1 + 8*k2 lives in CTA k2 at [b][Kl = k1][x]
+#pragma unroll
+    for (int k2 = 0; k2 < 8; ++k2) {
+      const uint32_t dst = mapa_u32(rv0 + uint32_t(((b * 8 + k1) * W + x) * sizeof(C)), uint32_t(k2));
+      st_async(dst, v[u][k2], mapa_u32(bar0, uint32_t(k2)));
+    }
+  }
+  // ---- phase 2: wait for all 64 b of this CTA's 8 K values ----------------
+  bool ok = false;
+  for (uint32_t it = 0; it < kColWaitLimit && !ok; ++it) {
+    uint32_t t;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(t)
+        : "r"(bar0)
+        : "memory");
+    ok = t != 0;
+  }
+  if (!ok && d.status) atomicExch(d.status, GBFFT_ERR_TIMEOUT_DEVICE);
+  const int K = 8 * r + g;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int blp = h + HS * u;
+#pragma unroll
+    for (int b1 = 0; b1 < 8; ++b1) v[u][b1] = rv[((8 * b1 + blp) * 8 + g) * W + x];
+    dft8(v[u]);
+    apply_powers8(v[u], w, 64 * blp);
+#pragma unroll
+    for (int kb1 = 0; kb1 < 8; ++kb1) sm[g * GP + (blp * 8 + kb1) * W + x] = v[u][kb1];
+  }
+  __syncthreads();
+  const T s = T(d.scale);
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int kb1 = h + HS * u;
+#pragma unroll
+    for (int blp = 0; blp < 8; ++blp) v[u][blp] = sm[g * GP + (blp * 8 + kb1) * W + x];
+    dft8(v[u]);
+#pragma unroll
+    for (int kb2 = 0; kb2 < 8; ++kb2) {
+      C e = v[u][kb2];
+      if (fl & F_SCALE) e = cscale(e, s);
+      if (fl & F_CONJ_OUT) e.y = -e.y;
+      out[int64_t(K + 64 * (kb1 + 8 * kb2)) * oes + x] = e;
+    }
+  }
+}
+
+template <typename T, int W, int U, int MINB>
+struct ColPushCfg {
+  static constexpr int threads = 64 * W / U;
+  static size_t smem() { return (size_t(8) * col_gp<W>() + size_t(64) * 8 * W) * sizeof(typename CxT<T>::type); }
+  static cudaError_t prepare() {
+    return cudaFuncSetAttribute(colfft4096_push_kernel<T, W, U, MINB>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem()));
+  }
+  static cudaError_t launch(const PassDesc& d, cudaStream_t s) {
+    const int64_t tiles = (d.ncols / W) * d.nbatch;
+    colfft4096_push_kernel<T, W, U, MINB><<<unsigned(tiles * 8), threads, smem(), s>>>(d);
+    return cudaGetLastError();
+  }
+};
+
+// Radix-16 variant: 4096 = 16 x 256 (y = 256a + b, k = K1 + 16k').
+//   phase 1: CTA r owns b in [32r, 32r+32): one DFT-16 over a per (b, x)
+//            straight from the loaded registers, twiddle W_4096^(b*K1), and
+//            K1 is pushed (st.async) to CTA K1/2, receive layout [b][K1 % 2][x].
+//   phase 2: CTA r' owns K1 in {2r', 2r'+1}: DFT-256 over b as 16 x 16
+//            (b = 16*beta + gamma, k' = kappa + 16*lambda) with one local
+//            exchange; output row K1 + 16*kappa + 256*lambda.
+// Three radix-16 stages and two twiddle stages per element.
+template <typename C>
+__device__ __forceinline__ void apply_powers16(C (&v)[16], const C* __restrict__ w, int m) {
+  // v[k] *= W_4096^(m*k): W^m, W^4m, W^8m loaded, the rest at most 3 products deep
+  const C w1 = tw_at(w, m & 4095), w4 = tw_at(w, (4 * m) & 4095), w8 = tw_at(w, (8 * m) & 4095);
+  const C w2 = cmul(w1, w1), w3 = cmul(w2, w1), w12 = cmul(w8, w4);
+  v[1] = cmul(v[1], w1);
+  v[2] = cmul(v[2], w2);
+  v[3] = cmul(v[3], w3);
+  v[4] = cmul(v[4], w4);
+  v[5] = cmul(v[5], cmul(w4, w1));
+  v[6] = cmul(v[6], cmul(w4, w2));
+  v[7] = cmul(v[7], cmul(w4, w3));
+  v[8] = cmul(v[8], w8);
+  v[9] = cmul(v[9], cmul(w8, w1));
+  v[10] = cmul(v[10], cmul(w8, w2));
+  v[11] = cmul(v[11], cmul(w8, w3));
+  v[12] = cmul(v[12], w12);
+  v[13] = cmul(v[13], cmul(w12, w1));
+  v[14] = cmul(v[14], cmul(w12, w2));
+  v[15] = cmul(v[15], cmul(w12, w3));
+}
+
+template <typename T, int W, int MINB>
+__global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
+    colfft4096_r16_kernel(const PassDesc d) {
+  using C = typename CxT<T>::type;
+  constexpr uint32_t kRecvBytes = 4096u * W / 8u * sizeof(C);  // 256 b x 2 K1 x W
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* rv = reinterpret_cast<C*>(smem_raw);  // [b][K1l][x], reused for the phase-2 exchange
+  __shared__ __align__(8) uint64_t rbar;
+  const int r = int(cg::this_cluster().block_rank());
+  const int64_t tile = int64_t(blockIdx.x) >> 3;
+  const int64_t tpb = d.ncols / W;
+  const int64_t bo = tile / tpb;
+  const int64_t x0 = (tile - bo * tpb) * W;
+  const C* __restrict__ in = static_cast<const C*>(d.in) + bo * d.in_bs + x0;
+  C* __restrict__ out = static_cast<C*>(d.out) + bo * d.out_bs + x0;
+  const C* __restrict__ w = static_cast<const C*>(d.tw);
+  const int64_t ies = d.in_es, oes = d.out_es;
+  const uint32_t fl = d.flags;
+  const int tid = threadIdx.x;
+  const int x = tid % W;
+  const int q = tid / W;  // 0..31
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&rbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  cluster_arrive_release();
+
+  // ---- phase 1: thread (x, bl = q): DFT-16 over a of column x, b = 32r + bl
+  const int b = 32 * r + q;
+  C v[16];
+#pragma unroll
+  for (int a = 0; a < 16; ++a) {
+    C e = in[int64_t(256 * a + b) * ies + x];
+    if (fl & F_CONJ_IN) e.y = -e.y;
+    v[a] = e;
+  }
+  dft16(v);
+  apply_powers16(v, w, b);  // W^(b*K1)
+  if (tid == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&rbar)),
+                 "r"(kRecvBytes)
+                 : "memory");
+  }
+  cluster_wait_acquire();
+  const uint32_t rv0 = smem_u32(rv), bar0 = smem_u32(&rbar);
+#pragma unroll
+  for (int K1 = 0; K1 < 16; ++K1) {
+    const uint32_t dst = mapa_u32(rv0 + uint32_t(((b * 2 + (K1 & 1)) * W + x) * sizeof(C)), uint32_t(K1 >> 1));
+    st_async(dst, v[K1], mapa_u32(bar0, uint32_t(K1 >> 1)));
+  }
+  // ---- phase 2: wait for the 256 b of this CTA's two K1 values ------------
+  bool ok = false;
+  for (uint32_t it = 0; it < kColWaitLimit && !ok; ++it) {
+    uint32_t t;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(t)
+        : "r"(bar0)
+        : "memory");
+    ok = t != 0;
+  }
+  if (!ok && d.status) atomicExch(d.status, GBFFT_ERR_TIMEOUT_DEVICE);
+  // stage 2: thread (x, K1l = q & 1, gamma = q >> 1): DFT-16 over beta
+  const int K1l = q & 1;
+  const int gamma = q >> 1;
+#pragma unroll
+  for (int beta = 0; beta < 16; ++beta) v[beta] = rv[((16 * beta + gamma) * 2 + K1l) * W + x];
+  dft16(v);
+  apply_powers16(v, w, 16 * gamma);  // W_256^(gamma*kappa)
+  __syncthreads();  // every stage-2 read of the receive buffer is done
+#pragma unroll
+  for (int kappa = 0; kappa < 16; ++kappa) rv[((kappa * 16 + gamma) * 2 + K1l) * W + x] = v[kappa];
+  __syncthreads();
+  // stage 3: thread (x, K1l, kappa = q >> 1): DFT-16 over gamma
+  const int kappa = q >> 1;
+#pragma unroll
+  for (int g = 0; g < 16; ++g) v[g] = rv[((kappa * 16 + g) * 2 + K1l) * W + x];
+  dft16(v);
+  const int K1 = 2 * r + K1l;
+  const T s = T(d.scale);
+#pragma unroll
+  for (int lambda = 0; lambda < 16; ++lambda) {
+    C e = v[lambda];
+    if (fl & F_SCALE) e = cscale(e, s);
+    if (fl & F_CONJ_OUT) e.y = -e.y;
+    out[int64_t(K1 + 16 * kappa + 256 * lambda) * oes + x] = e;
+  }
+}
+
+template <typename T, int W, int MINB>
+struct ColR16Cfg {
+  static constexpr int threads = 32 * W;
+  static size_t smem() { return size_t(512) * W * sizeof(typename CxT<T>::type); }
+  static cudaError_t prepare() {
+    return cudaFuncSetAttribute(colfft4096_r16_kernel<T, W, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(smem()));
+  }
+  static cudaError_t launch(const PassDesc& d, cudaStream_t s) {
+    const int64_t tiles = (d.ncols / W) * d.nbatch;
+    colfft4096_r16_kernel<T, W, MINB><<<unsigned(tiles * 8), threads, smem(), s>>>(d);
+    return cudaGetLastError();
+  }
+};
+
 template <typename T, int W> size_t col_smem() { return size_t(8) * col_gp<W>() * sizeof(typename CxT<T>::type); }
 
 template <typename T, int W, int U, int MINB>
@@ -239,6 +530,22 @@ struct ColCfg {
   X(2, float, 8, 2, 4)     \
   X(3, float, 16, 1, 1)
 
+// push variants (st.async into the owner's receive buffer)
+#define GBFFT_COLPUSH_TABLE(X) \
+  X(4, float, 8, 2, 3)         \
+  X(5, float, 8, 1, 3)         \
+  X(6, float, 16, 2, 1)        \
+  X(7, float, 8, 2, 2)
+
+// radix-16 variants (W, min CTAs per SM)
+#define GBFFT_COLR16_TABLE(X) \
+  X(8, float, 8, 3)           \
+  X(9, float, 16, 2)          \
+  X(10, float, 8, 4)          \
+  X(11, float, 16, 3)         \
+  X(12, float, 32, 1)         \
+  X(13, float, 16, 1)
+
 }  // namespace
 
 cudaError_t prepare_col_kernels() {
@@ -247,12 +554,24 @@ cudaError_t prepare_col_kernels() {
   if (e == cudaSuccess) e = ColCfg<T, W, U, MINB>::prepare();
   GBFFT_COL_TABLE(X)
 #undef X
+#define X(V, T, W, U, MINB) \
+  if (e == cudaSuccess) e = ColPushCfg<T, W, U, MINB>::prepare();
+  GBFFT_COLPUSH_TABLE(X)
+#undef X
+#define X(V, T, W, MINB) \
+  if (e == cudaSuccess) e = ColR16Cfg<T, W, MINB>::prepare();
+  GBFFT_COLR16_TABLE(X)
+#undef X
   if (e == cudaSuccess) e = ColCfg<double, 16, 2, 1>::prepare();
   return e;
 }
 
 int col_tile_width(int variant) {
-  return (variant == 1 || variant == 2) ? 8 : 16;
+  switch (variant) {
+    case 0: case 3: case 6: case 9: case 11: case 13: return 16;
+    case 12: return 32;
+    default: return 8;
+  }
 }
 
 cudaError_t launch_col4096(const PassDesc& d, bool dbl, cudaStream_t s) {
@@ -260,6 +579,14 @@ cudaError_t launch_col4096(const PassDesc& d, bool dbl, cudaStream_t s) {
 #define X(V, T, W, U, MINB) \
   if (d.col_variant == V) return ColCfg<T, W, U, MINB>::launch(d, s);
   GBFFT_COL_TABLE(X)
+#undef X
+#define X(V, T, W, U, MINB) \
+  if (d.col_variant == V) return ColPushCfg<T, W, U, MINB>::launch(d, s);
+  GBFFT_COLPUSH_TABLE(X)
+#undef X
+#define X(V, T, W, MINB) \
+  if (d.col_variant == V) return ColR16Cfg<T, W, MINB>::launch(d, s);
+  GBFFT_COLR16_TABLE(X)
 #undef X
   return cudaErrorInvalidValue;
 }

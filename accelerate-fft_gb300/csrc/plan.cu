@@ -647,11 +647,12 @@ int build_plan(gbfft_plan* p, bool dry) {
     // measured defaults on GB300 (fft2D 4096^2): single-buffered rows at
     // 4 CTAs/SM, 8-column cluster tiles at 4 CTAs/SM; env overrides for A/B
     ps.d.row_variant = 1;
-    ps.d.col_variant = 2;
+    ps.d.col_variant = 9;
     if (const char* rv = std::getenv("GBFFT_ROW_VARIANT")) ps.d.row_variant = std::atoi(rv) & 1;
-    if (const char* cv = std::getenv("GBFFT_COL_VARIANT")) ps.d.col_variant = std::atoi(cv) & 3;
+    if (const char* cv = std::getenv("GBFFT_COL_VARIANT")) ps.d.col_variant = std::atoi(cv) & 15;
+    if (ps.d.col_variant > 13) ps.d.col_variant = 9;
     if (ps.d.kernel == K_COL4096 && ps.d.ncols % col_tile_width(ps.d.col_variant) != 0)
-      ps.d.col_variant = 1;  // 8-column tiles
+      ps.d.col_variant = 8;  // 8-column tiles
     if (ps.tw_off >= 0) ps.d.tw = base + ps.tw_off;
     if (ps.tw4lo_off >= 0) ps.d.tw4_lo = base + ps.tw4lo_off;
     if (ps.tw4hi_off >= 0) ps.d.tw4_hi = base + ps.tw4hi_off;

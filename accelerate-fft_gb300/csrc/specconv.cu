@@ -205,7 +205,7 @@ int gbfft_specconv_plan_create(gbfft_specconv_plan** out, int64_t batch, int64_t
     if (ps->tw_off >= 0) ps->d.tw = tb + ps->tw_off;
     ps->d.use_tma = 1;
     ps->d.row_variant = 1;
-    ps->d.col_variant = 2;
+    ps->d.col_variant = 9;
   }
   p->tmp_bytes = size_t(batch) * size_t(p->N) * (dbl ? 16 : 8);
   if (cudaMalloc(&p->d_tmp, p->tmp_bytes) != cudaSuccess) return GBFFT_ERR_ALLOC;

@@ -256,7 +256,7 @@ def run_gbfft(args, wl):
     sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
     if sampler:
         sampler.start()
-        time.sleep(0.3)
+        time.sleep(1.0)  # let nvidia-smi finish starting before the timed region
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(npass + 1)] for _ in range(args.steps)]
     torch.cuda.synchronize()
     for k in range(args.steps):
@@ -413,7 +413,7 @@ def run_ragged(args, wl):
     sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
     if sampler:
         sampler.start()
-        time.sleep(0.3)
+        time.sleep(1.0)
     ts = timed(False, args.steps, args.warmup)
     if world > 1:
         torch.distributed.barrier()
@@ -559,7 +559,7 @@ def run_specconv(args, wl):
     sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
     if sampler:
         sampler.start()
-        time.sleep(0.3)
+        time.sleep(1.0)
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     for k in range(args.steps):
         step(evs[k])

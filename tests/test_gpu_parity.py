@@ -287,8 +287,11 @@ def test_fault_injection_alloc(gbfft_lib, monkeypatch):
 
 # ---- kernel variants: TMA-fed rows, register rows, cluster columns, generic --
 @pytest.mark.parametrize("disable,rowv,colv", [("", "1", "2"), ("", "0", "0"), ("tma", "0", "1"),
-                                               ("", "1", "3"), ("row", "1", "2"), ("cluster", "1", "2"),
-                                               ("tma,row,cluster", "0", "0")])
+                                               ("", "1", "3"), ("", "1", "4"), ("", "1", "5"),
+                                               ("", "1", "6"), ("", "1", "7"), ("", "1", "8"),
+                                               ("", "1", "9"), ("", "1", "10"), ("", "1", "11"),
+                                               ("", "1", "12"), ("", "1", "13"), ("row", "1", "2"),
+                                               ("cluster", "1", "2"), ("tma,row,cluster", "0", "0")])
 def test_kernel_variants_agree(gbfft_lib, monkeypatch, disable, rowv, colv):
     g = gbfft_lib
     from gbfft import _lib as L
