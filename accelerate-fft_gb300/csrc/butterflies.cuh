@@ -6,6 +6,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 namespace gbfft {
 
 template <typename T> struct CxT;
@@ -166,6 +168,37 @@ template <int R, typename C> __device__ __forceinline__ void dft(C* v) {
   else if constexpr (R == 8) dft8(v);
   else if constexpr (R == 16) dft16(v);
   else dft_odd<R>(v);
+}
+
+// L2 eviction-priority hints for streaming loads and for stores a later pass
+// reads back.
+__device__ __forceinline__ uint64_t l2_policy_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float2 ld_l2hint(const float2* a, uint64_t pol) {
+  float2 v;
+  asm volatile("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double2 ld_l2hint(const double2* a, uint64_t pol) {
+  double2 v;
+  asm volatile("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st_l2hint(float2* a, float2 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(a), "f"(v.x), "f"(v.y), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void st_l2hint(double2* a, double2 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(a), "d"(v.x), "d"(v.y), "l"(pol)
+               : "memory");
 }
 
 }  // namespace gbfft

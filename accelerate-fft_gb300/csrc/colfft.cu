@@ -429,9 +429,12 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
   // ---- phase 1: thread (x, bl = q): DFT-16 over a of column x, b = 32r + bl
   const int b = 32 * r + q;
   C v[16];
+  const bool stream_in = (fl & F_L2_IN_FIRST) != 0;
+  const uint64_t ipol = stream_in ? l2_policy_first() : 0;
 #pragma unroll
   for (int a = 0; a < 16; ++a) {
-    C e = in[int64_t(256 * a + b) * ies + x];
+    const C* p = in + int64_t(256 * a + b) * ies + x;
+    C e = stream_in ? ld_l2hint(p, ipol) : *p;
     if (fl & F_CONJ_IN) e.y = -e.y;
     v[a] = e;
   }

@@ -33,6 +33,8 @@ enum PassFlags : uint32_t {
   F_CHIRP_OUT = 1u << 9,   // conjugate then multiply by chirp[l] on store
   F_TRUNC_OUT = 1u << 10,  // store only logical output index l < n_out
   F_SPEC = 1u << 11,       // in-kernel spectral multiply: DFT, * filter[l], conj, DFT
+  F_L2_IN_FIRST = 1u << 12,  // loads: L2 evict_first (input read once)
+  F_L2_OUT_LAST = 1u << 13,  // stores: L2 evict_last (a later pass reads them back)
 };
 
 // Kernel families a pass can run on.

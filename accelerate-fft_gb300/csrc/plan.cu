@@ -638,6 +638,14 @@ int build_plan(gbfft_plan* p, bool dry) {
     p->scratch_bytes = b1 + size_t(s2) * eb;
     if (cudaMalloc(&p->d_scratch, p->scratch_bytes) != cudaSuccess) return GBFFT_ERR_ALLOC;
   }
+  // L2 policy: a pass whose output a later pass reads back stores it with
+  // evict_last; every pass after the first streams its input (evict_first)
+  if (p->passes.size() > 1 && !feature_disabled("l2hint")) {
+    for (size_t i = 0; i < p->passes.size(); ++i) {
+      if (i + 1 < p->passes.size()) p->passes[i].d.flags |= F_L2_OUT_LAST;
+      p->passes[i].d.flags |= F_L2_IN_FIRST;
+    }
+  }
   unsigned char* base = static_cast<unsigned char*>(p->d_tables);
   p->d_status = reinterpret_cast<int*>(base + status_off);
   const bool tma = !feature_disabled("tma");

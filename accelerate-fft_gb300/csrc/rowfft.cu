@@ -244,18 +244,25 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft1_kernel(const PassD
   const C* __restrict__ in = static_cast<const C*>(d.in) + row * d.in_cs;
   C* __restrict__ out = static_cast<C*>(d.out) + row * d.out_cs;
   C v[E];
+  const bool stream_in = (fl & F_L2_IN_FIRST) != 0;
+  const uint64_t ipol = stream_in ? l2_policy_first() : 0;
 #pragma unroll
   for (int q = 0; q < E / R0; ++q)
 #pragma unroll
     for (int r = 0; r < R0; ++r) {
       C x = cmake<C>(T(0), T(0));
-      if (ok) x = in[t + TH * (q + r * (E / R0))];
+      if (ok) {
+        const C* a = in + t + TH * (q + r * (E / R0));
+        x = stream_in ? ld_l2hint(a, ipol) : *a;
+      }
       if (fl & F_CONJ_IN) x.y = -x.y;
       v[q * R0 + r] = x;
     }
   row_stages1<N, E, 1, 0>(v, b, static_cast<const C*>(d.tw), t, RL<Rs...>{});
   if (!ok) return;
   const T s = T(d.scale);
+  const bool keep = (fl & F_L2_OUT_LAST) != 0;
+  const uint64_t pol = keep ? l2_policy_last() : 0;
 #pragma unroll
   for (int q = 0; q < E / RZ; ++q)
 #pragma unroll
@@ -263,7 +270,11 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft1_kernel(const PassD
       C x = v[q * RZ + r];
       if (fl & F_SCALE) x = cscale(x, s);
       if (fl & F_CONJ_OUT) x.y = -x.y;
-      out[t + TH * (q + r * (E / RZ))] = x;
+      C* o = out + t + TH * (q + r * (E / RZ));
+      if (keep)
+        st_l2hint(o, x, pol);
+      else
+        *o = x;
     }
 }
 
