@@ -43,6 +43,7 @@ enum KernelId : int {
   K_ROW = 1,      // register-resident contiguous-row kernel (specialised lengths)
   K_COL4096 = 2,  // 8-CTA cluster kernel for stride-S axes of length 4096
   K_ROW_TC = 3,   // contiguous rows, radix-16 stages as split-FP16 tensor-core GEMMs
+  K_STRIDED = 4,  // register-resident strided pencils, W adjacent columns per CTA
 };
 
 struct StageInfo {
@@ -109,6 +110,10 @@ cudaError_t prepare_row_kernels();
 cudaError_t launch_row(const PassDesc& d, bool dbl, cudaStream_t s);
 cudaError_t prepare_col_kernels();
 bool row_tc_available(int n);
+bool str_kernel_available(int n, bool dbl);
+int str_kernel_width(bool dbl);
+cudaError_t prepare_str_kernels();
+cudaError_t launch_str(const PassDesc& d, bool dbl, cudaStream_t s);
 cudaError_t prepare_row_tc_kernels();
 cudaError_t launch_row_tc(const PassDesc& d, cudaStream_t s);
 cudaError_t launch_col4096(const PassDesc& d, bool dbl, cudaStream_t s);

@@ -33,6 +33,8 @@ cudaError_t prepare_kernels() {
   if (e != cudaSuccess) return e;
   e = prepare_row_tc_kernels();
   if (e != cudaSuccess) return e;
+  e = prepare_str_kernels();
+  if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(pencil_kernel<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   if (e != cudaSuccess) return e;
@@ -44,6 +46,7 @@ cudaError_t launch_pass(const PassDesc& d, bool is_double, cudaStream_t stream) 
   if (d.kernel == K_ROW) return launch_row(d, is_double, stream);
   if (d.kernel == K_COL4096) return launch_col4096(d, is_double, stream);
   if (d.kernel == K_ROW_TC) return launch_row_tc(d, stream);
+  if (d.kernel == K_STRIDED) return launch_str(d, is_double, stream);
   const int grid = pass_grid(d);
   if (grid <= 0) return cudaSuccess;
   const size_t smem = pass_smem_bytes(d, is_double);

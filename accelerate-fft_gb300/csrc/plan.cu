@@ -373,6 +373,11 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
       d.kernel = K_COL4096;
       ps.tw_off = int64_t(B.roots_for(4096));
       kname = "col4096-cluster8";
+    } else if (ax.cs == 1 && ax.es != 1 && str_kernel_available(int(ax.n), dbl) &&
+               ax.ncols % str_kernel_width(dbl) == 0 && !feature_disabled("strided")) {
+      d.kernel = K_STRIDED;
+      d.W = str_kernel_width(dbl);
+      kname = "strided";
     }
     ps.src = src;
     ps.dst = R_OUT;

@@ -410,6 +410,157 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_tma_kernel(const Pa
   }
 }
 
+// ---- strided pencils (the y / z axes of fft2D / fft3D, spectral product) -----
+// A CTA transforms W adjacent columns of a stride-es axis of length N: thread
+// (x, t) holds elements t + TH*m of column x in registers, global accesses are
+// W-column row segments, and the exchanges use a column-interleaved layout
+// [i][x] (x fastest), which keeps every Stockham access pattern free of bank
+// conflicts.  With F_SPEC the kernel multiplies the spectrum by filter[k*S +
+// column], conjugates, and runs the same stages again straight from
+// registers (the output index set of a transform is the input index set of
+// the next), giving the forward z DFT, product and first inverse axis of the
+// spectral convolution in one pass.
+template <int N, int E, int NS, int R, int W, typename C>
+__device__ __forceinline__ void str_write(const C (&v)[E], C* buf, int t, int x) {
+  constexpr int TH = N / E;
+  constexpr int Q = E / R;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int j = t + TH * q;
+    const int p = j % NS;
+    const int base = (j - p) * R + p;
+#pragma unroll
+    for (int r = 0; r < R; ++r) buf[(base + r * NS) * W + x] = v[q * R + r];
+  }
+}
+template <int N, int E, int R, int W, typename C>
+__device__ __forceinline__ void str_read(C (&v)[E], const C* buf, int t, int x) {
+  constexpr int TH = N / E;
+  constexpr int Q = E / R;
+#pragma unroll
+  for (int q = 0; q < Q; ++q)
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[q * R + r] = buf[(t + TH * q + r * (N / R)) * W + x];
+}
+template <int N, int E, int NS, int OFF, int W, typename C, int R, int... Rest>
+__device__ __forceinline__ void str_stages(C (&v)[E], C* b, const C* __restrict__ tw, int t, int x,
+                                           RL<R, Rest...>) {
+  row_compute<N, E, NS, R>(v, tw + OFF, t);
+  if constexpr (sizeof...(Rest) > 0) {
+    str_write<N, E, NS, R, W>(v, b, t, x);
+    __syncthreads();
+    constexpr int R2 = rl_first(RL<Rest...>{});
+    str_read<N, E, R2, W>(v, b, t, x);
+    __syncthreads();
+    str_stages<N, E, NS * R, OFF + NS * even_up<R>(), W>(v, b, tw, t, x, RL<Rest...>{});
+  }
+}
+
+template <typename T, int N, int W, int MINB, int... Rs>
+__global__ void __launch_bounds__(W*(N / 16), MINB) strfft_kernel(const PassDesc d) {
+  using C = typename CxT<T>::type;
+  constexpr int E = 16;
+  constexpr int TH = N / E;
+  constexpr int R0 = rl_first(RL<Rs...>{});
+  constexpr int RZ = rl_last(RL<Rs...>{});
+  static_assert(R0 == 16 || E % R0 == 0, "radix");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* b = reinterpret_cast<C*>(smem_raw);
+  const int x = threadIdx.x % W;
+  const int t = threadIdx.x / W;
+  const int64_t tiles = (d.ncols + W - 1) / W;
+  const int64_t bq = int64_t(blockIdx.x) / tiles;
+  const int64_t c0 = (int64_t(blockIdx.x) - bq * tiles) * W;
+  const int64_t b_hi = bq / d.nb_lo;
+  const int64_t b_lo = bq - b_hi * d.nb_lo;
+  const int64_t col = c0 + x;
+  const bool ok = col < d.ncols;
+  const uint32_t fl = d.flags;
+  const C* __restrict__ in = static_cast<const C*>(d.in) + b_lo * d.in_bs + b_hi * d.in_bs2 + col * d.in_cs;
+  C* __restrict__ out = static_cast<C*>(d.out) + b_lo * d.out_bs + b_hi * d.out_bs2 + col * d.out_cs;
+  const C* __restrict__ tw = static_cast<const C*>(d.tw);
+  const bool stream_in = (fl & F_L2_IN_FIRST) != 0;
+  const uint64_t ipol = stream_in ? l2_policy_first() : 0;
+  C v[E];
+#pragma unroll
+  for (int q = 0; q < E / R0; ++q)
+#pragma unroll
+    for (int r = 0; r < R0; ++r) {
+      C e = cmake<C>(T(0), T(0));
+      if (ok) {
+        const C* a = in + int64_t(t + TH * (q + r * (E / R0))) * d.in_es;
+        e = stream_in ? ld_l2hint(a, ipol) : *a;
+      }
+      if (fl & F_CONJ_IN) e.y = -e.y;
+      v[q * R0 + r] = e;
+    }
+  str_stages<N, E, 1, 0, W>(v, b, tw, t, x, RL<Rs...>{});
+  if (fl & F_SPEC) {
+    // v[q*RZ + r] holds X[k], k = t + TH*(q + r*E/RZ); the next transform's
+    // first stage wants x[t + TH*(q' + r'*E/R0)] in v[q'*R0 + r']
+    const C* __restrict__ filt = static_cast<const C*>(d.filter);
+    C u[E];
+#pragma unroll
+    for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+      for (int r = 0; r < RZ; ++r) {
+        const int m = q + r * (E / RZ);
+        const int k = t + TH * m;
+        const C h = ok ? filt[int64_t(k) * d.lout_es + col * d.lout_cs] : cmake<C>(T(0), T(0));
+        const C z = cconj(cmul(v[q * RZ + r], h));
+        // slot of m in the first-stage ordering: m = q' + r' * (E / R0)
+        u[(m % (E / R0)) * R0 + m / (E / R0)] = z;
+      }
+#pragma unroll
+    for (int i = 0; i < E; ++i) v[i] = u[i];
+    __syncthreads();
+    str_stages<N, E, 1, 0, W>(v, b, tw, t, x, RL<Rs...>{});
+  }
+  if (!ok) return;
+  const T s = T(d.scale);
+  const bool keep = (fl & F_L2_OUT_LAST) != 0;
+  const uint64_t pol = keep ? l2_policy_last() : 0;
+#pragma unroll
+  for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+    for (int r = 0; r < RZ; ++r) {
+      C e = v[q * RZ + r];
+      if (fl & F_SCALE) e = cscale(e, s);
+      if (fl & F_CONJ_OUT) e.y = -e.y;
+      C* o = out + int64_t(t + TH * (q + r * (E / RZ))) * d.out_es;
+      if (keep)
+        st_l2hint(o, e, pol);
+      else
+        *o = e;
+    }
+}
+
+template <typename T, int N, int W, int MINB, int... Rs>
+struct StrCfg {
+  static constexpr int threads = W * (N / 16);
+  static size_t smem() { return size_t(N) * W * sizeof(typename CxT<T>::type); }
+  static cudaError_t prepare() {
+    return cudaFuncSetAttribute(strfft_kernel<T, N, W, MINB, Rs...>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(smem()));
+  }
+  static cudaError_t launch(const PassDesc& d, cudaStream_t s) {
+    const int64_t tiles = (d.ncols + W - 1) / W;
+    strfft_kernel<T, N, W, MINB, Rs...><<<unsigned(tiles * d.nbatch), threads, smem(), s>>>(d);
+    return cudaGetLastError();
+  }
+};
+
+// (type, N, W, min CTAs per SM, radices = factor_device(N))
+#define GBFFT_STR_TABLE(X)                 \
+  X(float, 256, 16, 3, 16, 16)             \
+  X(float, 512, 16, 2, 16, 16, 2)          \
+  X(float, 1024, 16, 1, 16, 16, 4)         \
+  X(float, 128, 16, 4, 16, 8)              \
+  X(float, 64, 16, 4, 16, 4)               \
+  X(double, 256, 8, 2, 16, 16)             \
+  X(double, 512, 8, 1, 16, 16, 2)          \
+  X(double, 1024, 8, 1, 16, 16, 4)
+
 // ---- split-FP16 tensor-core variant (Complex Float) --------------------------
 // Every radix-16 stage runs as a GEMM on the 5th-generation tensor cores:
 // the 128 butterflies of a warpgroup form the rows of A (128 x 32: real then
@@ -764,6 +915,33 @@ cudaError_t prepare_row_kernels() {
   GBFFT_ROW_TABLE(X)
 #undef X
   return e;
+}
+
+bool str_kernel_available(int n, bool dbl) {
+#define X(T, N, W, MINB, ...) \
+  if (n == N && dbl == (sizeof(T) == 8)) return true;
+  GBFFT_STR_TABLE(X)
+#undef X
+  return false;
+}
+
+int str_kernel_width(bool dbl) { return dbl ? 8 : 16; }
+
+cudaError_t prepare_str_kernels() {
+  cudaError_t e = cudaSuccess;
+#define X(T, N, W, MINB, ...) \
+  if (e == cudaSuccess) e = StrCfg<T, N, W, MINB, __VA_ARGS__>::prepare();
+  GBFFT_STR_TABLE(X)
+#undef X
+  return e;
+}
+
+cudaError_t launch_str(const PassDesc& d, bool dbl, cudaStream_t s) {
+#define X(T, N, W, MINB, ...) \
+  if (d.n == N && dbl == (sizeof(T) == 8)) return StrCfg<T, N, W, MINB, __VA_ARGS__>::launch(d, s);
+  GBFFT_STR_TABLE(X)
+#undef X
+  return cudaErrorInvalidValue;
 }
 
 bool row_tc_available(int n) {

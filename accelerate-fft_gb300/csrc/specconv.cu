@@ -181,7 +181,9 @@ int gbfft_specconv_plan_create(gbfft_specconv_plan** out, int64_t batch, int64_t
   p->px = v[0];
   p->py = v[1];
   p->pz = v[2];
-  p->pz.d.kernel = K_PENCIL;  // the spectral product runs inside the generic pencil body
+  // the spectral product runs inside the strided register kernel when the
+  // z length has one, else inside the generic pencil body
+  if (p->pz.d.kernel != K_STRIDED) p->pz.d.kernel = K_PENCIL;
   p->pz.d.flags |= F_SPEC;
   p->pz.d.lout_es = S;
   p->pz.d.lout_cs = 1;

@@ -290,7 +290,8 @@ def test_fault_injection_alloc(gbfft_lib, monkeypatch):
                                                ("", "1", "3"), ("", "1", "4"), ("", "1", "5"),
                                                ("", "1", "6"), ("", "1", "7"), ("", "1", "8"),
                                                ("", "1", "9"), ("", "1", "10"), ("", "1", "11"),
-                                               ("", "1", "12"), ("", "1", "13"), ("row", "1", "2"),
+                                               ("", "1", "12"), ("", "1", "13"), ("strided", "1", "9"),
+                                               ("row", "1", "2"),
                                                ("cluster", "1", "2"), ("tma,row,cluster", "0", "0")])
 def test_kernel_variants_agree(gbfft_lib, monkeypatch, disable, rowv, colv):
     g = gbfft_lib
@@ -303,7 +304,10 @@ def test_kernel_variants_agree(gbfft_lib, monkeypatch, disable, rowv, colv):
              ((64, 1000), "many", np.complex64), ((5, 8192), "many", np.complex64),
              ((41, 256), "many", np.complex64), ((3, 2048), "full", np.complex64),
              ((7, 512), "many", np.complex64), ((33, 4096), "many", np.complex128),
-             ((2, 4096, 32), "full", np.complex64)]
+             ((2, 4096, 32), "full", np.complex64), ((256, 48), "full", np.complex64),
+             ((1024, 64), "full", np.complex64), ((3, 256, 32), "full", np.complex64),
+             ((128, 16, 64), "full", np.complex64), ((512, 16), "full", np.complex128),
+             ((64, 64, 16), "full", np.complex64)]
     for shape, kind, dt in cases:
         x = uniform_complex(rng, shape, dt)
         plan = g.Plan(shape, kind=kind, dtype=torch.complex64 if dt == np.complex64 else torch.complex128)
