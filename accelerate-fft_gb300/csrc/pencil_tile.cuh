@@ -179,7 +179,7 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
     C v = res[c * d.pitch + spad(kk)];
     if (fl & F_TW4) {
       const int64_t e = (fl & F_TW4_BATCH) ? b : col;
-      const int64_t t = (e * int64_t(kk)) % d.tw4_n;
+      const int64_t t = e * int64_t(kk);  // e < N/n and kk < n, so t < N
       v = cmul(v, cmul(tw4_hi[t >> d.tw4_shift], tw4_lo[t & tw4_mask]));
     }
     if (fl & F_FILTER_OUT) v = cconj(cmul(v, filt[l]));

@@ -28,6 +28,7 @@
 #include "gbfft.h"
 #include "gbfft_internal.h"
 #include "plan_internal.h"
+#include "strided_tile.cuh"
 
 namespace gbfft {
 
@@ -320,18 +321,32 @@ static PassSpec blank_pass() {
   return ps;
 }
 
+// Strided halves (consecutive columns adjacent in the source) run on the
+// register-resident strided kernel when their length has one.
+static void use_strided(PassSpec& ps, bool dbl) {
+  PassDesc& d = ps.d;
+  if (d.in_cs == 1 && d.in_es != 1 && str_kernel_available(d.n, dbl) && str_ops_supported(d.flags) &&
+      !feature_disabled("strided")) {
+    d.kernel = K_STRIDED;
+    d.W = str_kernel_width(dbl);
+  }
+}
+
 static int cap_for(bool dbl) { return dbl ? kCapC64 : kCapC32; }
 
 // Split n = n1*n2 (n1 strided first pass, n2 second) with both <= cap,
 // n1 as close to sqrt(n) as possible.
-static bool split_four_step(int64_t n, int cap, int64_t& n1, int64_t& n2) {
+static bool split_four_step(int64_t n, int cap, int64_t& n1, int64_t& n2, bool dbl = false) {
   int64_t best = 0;
   double bestd = 1e300;
   for (int64_t a = 2; a <= cap && a < n; ++a) {
     if (n % a) continue;
     const int64_t b = n / a;
     if (b > cap || b < 2) continue;
-    const double dd = std::fabs(std::log(double(a)) - std::log(double(b)));
+    // balanced halves, and halves that have a register-resident strided kernel
+    double dd = std::fabs(std::log(double(a)) - std::log(double(b)));
+    if (str_kernel_available(int(a), dbl)) dd -= 2.0;
+    if (str_kernel_available(int(b), dbl)) dd -= 2.0;
     if (dd < bestd) {
       bestd = dd;
       best = a;
@@ -390,7 +405,7 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
 
   if (is_fast_length(ax.n)) {
     int64_t n1, n2;
-    if (!split_four_step(ax.n, cap, n1, n2)) return GBFFT_ERR_UNSUPPORTED;
+    if (!split_four_step(ax.n, cap, n1, n2, dbl)) return GBFFT_ERR_UNSUPPORTED;
     PassSpec p1 = blank_pass(), p2 = blank_pass();
     if (!B.stages_for(int(n1), p1) || !B.stages_for(int(n2), p2)) return GBFFT_ERR_UNSUPPORTED;
     B.tw4_for(ax.n, p1);
@@ -440,6 +455,8 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     }
     choose_tile(p1, dbl);
     choose_tile(p2, dbl);
+    use_strided(p1, dbl);
+    use_strided(p2, dbl);
     p1.src = src;
     p1.dst = mid;
     p2.src = mid;
@@ -485,7 +502,7 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
   if (ax.es != 1) return GBFFT_ERR_UNSUPPORTED;
   if (ax.outer > 1 && ax.os != ax.ncols * ax.cs) return GBFFT_ERR_UNSUPPORTED;
   int64_t m1, m2;
-  if (!split_four_step(m, cap, m1, m2)) return GBFFT_ERR_UNSUPPORTED;
+  if (!split_four_step(m, cap, m1, m2, dbl)) return GBFFT_ERR_UNSUPPORTED;
   const int64_t rows = ax.ncols * ax.outer;
   scratch1 = std::max(scratch1, rows * m);
   scratch2 = std::max(scratch2, rows * m);
@@ -557,6 +574,7 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
   p[3].dst = R_OUT;
   for (int i = 0; i < 4; ++i) {
     choose_tile(p[i], dbl);
+    use_strided(p[i], dbl);
     passes.push_back(p[i]);
   }
   std::snprintf(buf, sizeof buf, "[n=%lld bluestein m=%lld=%lldx%lld 4-pass]", (long long)ax.n,

@@ -30,6 +30,7 @@
 #include "gbfft.h"
 #include "pencil_tile.cuh"
 #include "plan_internal.h"
+#include "strided_tile.cuh"
 
 namespace gbfft {
 
@@ -71,8 +72,19 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
   return v;
 }
 
+// Separate (not inlined) bodies per tile kind, so the register allocation of
+// one kind does not inflate the others.
+template <typename T, int N, int W, int... Rs>
+__device__ __noinline__ void ragged_str(const PassDesc& d, int64_t tile, unsigned char* smem) {
+  str_tile_dispatch<T, N, W, Rs...>(d, tile, smem);
+}
 template <typename T>
-__global__ void __launch_bounds__(kRaggedThreads) ragged_kernel(const RaggedArgs a) {
+__device__ __noinline__ void ragged_pencil(const PassDesc& d, int64_t tile, unsigned char* smem) {
+  pencil_tile<T>(d, tile, smem);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRaggedThreads, 2) ragged_kernel(const RaggedArgs a) {
   using C = typename CxT<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int kDescBytes = (int(sizeof(PassDesc)) + 127) & ~127;
@@ -124,7 +136,20 @@ __global__ void __launch_bounds__(kRaggedThreads) ragged_kernel(const RaggedArgs
     }
     __syncthreads();
     if (s_timeout) break;
-    pencil_tile<T>(d, task.count ? 0 : task.tile, bufs);
+    const int64_t tl = task.count ? 0 : task.tile;
+    if (d.kernel == K_STRIDED) {
+      // W = 4096 / N keeps every instantiation at kRaggedThreads threads
+      switch (d.n) {
+        case 64: ragged_str<T, 64, 64, 16, 4>(d, tl, bufs); break;
+        case 128: ragged_str<T, 128, 32, 16, 8>(d, tl, bufs); break;
+        case 256: ragged_str<T, 256, 16, 16, 16>(d, tl, bufs); break;
+        case 512: ragged_str<T, 512, 8, 16, 16, 2>(d, tl, bufs); break;
+        case 1024: ragged_str<T, 1024, 4, 16, 16, 4>(d, tl, bufs); break;
+        default: break;
+      }
+    } else {
+      ragged_pencil<T>(d, tl, bufs);
+    }
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0 && task.signal >= 0) atomicAdd(&a.counters[task.signal], 1);
@@ -167,10 +192,20 @@ struct gbfft_ragged_plan {
 
 namespace {
 
-// Tile width for a ragged pass: at most `budget` elements per tile.
+// Tile width for a ragged pass: at most `budget` elements per tile.  Strided
+// halves whose length has a register kernel use it with W = 4096 / n.
 void ragged_tile(PassSpec& ps, bool dbl, int budget, int64_t group) {
   PassDesc& d = ps.d;
   const int n = d.n;
+  if (group == 0 && d.in_cs == 1 && d.in_es != 1 && (n == 64 || n == 128 || n == 256 || n == 512 || n == 1024) &&
+      str_ops_supported(d.flags) && !feature_disabled("strided")) {
+    d.kernel = K_STRIDED;
+    d.W = 4096 / n;
+    d.threads = kRaggedThreads;
+    d.pitch = n;
+    return;
+  }
+  d.kernel = K_PENCIL;
   int pitch = n + (n >> 4) + 1;
   if (pitch % 2 == 0) ++pitch;
   d.pitch = pitch;
@@ -396,7 +431,9 @@ int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64
     if (ps.chirp_off >= 0) ps.d.chirp = tb + ps.chirp_off;
     if (ps.filter_off >= 0) ps.d.filter = tb + ps.filter_off;
     ps.d.status = p->d_status;
-    smem_max = std::max(smem_max, pass_smem_bytes(ps.d, dbl));
+    const size_t sb = ps.d.kernel == K_STRIDED ? size_t(ps.d.n) * ps.d.W * (dbl ? 16 : 8)
+                                               : pass_smem_bytes(ps.d, dbl);
+    smem_max = std::max(smem_max, sb);
     hdescs.push_back(ps.d);
   }
   const size_t desc_bytes = (sizeof(PassDesc) + 127) & ~size_t(127);

@@ -26,132 +26,11 @@
 
 #include "butterflies.cuh"
 #include "gbfft_internal.h"
+#include "strided_tile.cuh"
 
 namespace gbfft {
 
 namespace {
-
-__device__ __forceinline__ int swz(int i) { return i ^ (((i >> 4) & 7) << 1); }
-
-template <int... Rs> struct RL {};
-template <int R, int... Rest> constexpr int rl_first(RL<R, Rest...>) { return R; }
-template <int R> constexpr int rl_last(RL<R>) { return R; }
-template <int R, int R2, int... Rest> constexpr int rl_last(RL<R, R2, Rest...>) {
-  return rl_last(RL<R2, Rest...>{});
-}
-template <int R> constexpr int even_up() { return R + (R & 1); }
-// row pitch of the exchange buffers: a multiple of 16 so the swizzle stays
-// inside the row and 16-byte stores stay aligned
-template <int N> constexpr int row_pitch() { return (N + 15) & ~15; }
-
-// twiddles W^{p*r}, r < R, of one butterfly (table stride even_up(R))
-template <int R>
-__device__ __forceinline__ void load_tw(float2 (&w)[R + 1], const float2* __restrict__ base) {
-  const float4* b4 = reinterpret_cast<const float4*>(base);
-#pragma unroll
-  for (int k = 0; k < even_up<R>() / 2; ++k) {
-    const float4 q = __ldg(b4 + k);
-    w[2 * k] = make_float2(q.x, q.y);
-    if (2 * k + 1 <= R) w[2 * k + 1] = make_float2(q.z, q.w);
-  }
-}
-template <int R>
-__device__ __forceinline__ void load_tw(double2 (&w)[R + 1], const double2* __restrict__ base) {
-#pragma unroll
-  for (int r = 1; r < R; ++r) w[r] = __ldg(base + r);
-}
-
-// Complex Float twiddles derived from a few table entries: W^p, W^4p, W^8p
-// are loaded and the other powers formed with at most three complex
-// multiplications (a few ulp), which keeps the L1 traffic per butterfly at
-// three 8-byte loads instead of R-1.
-template <int R>
-__device__ __forceinline__ void derive_tw(float2 (&w)[R + 1], const float2* __restrict__ base) {
-  if constexpr (R == 16) {
-    w[1] = __ldg(base + 1);
-    w[4] = __ldg(base + 4);
-    w[8] = __ldg(base + 8);
-    w[2] = cmul(w[1], w[1]);
-    w[3] = cmul(w[2], w[1]);
-    w[5] = cmul(w[4], w[1]);
-    w[6] = cmul(w[4], w[2]);
-    w[7] = cmul(w[4], w[3]);
-    w[9] = cmul(w[8], w[1]);
-    w[10] = cmul(w[8], w[2]);
-    w[11] = cmul(w[8], w[3]);
-    w[12] = cmul(w[8], w[4]);
-    w[13] = cmul(w[12], w[1]);
-    w[14] = cmul(w[12], w[2]);
-    w[15] = cmul(w[12], w[3]);
-  } else if constexpr (R == 8) {
-    w[1] = __ldg(base + 1);
-    w[4] = __ldg(base + 4);
-    w[2] = cmul(w[1], w[1]);
-    w[3] = cmul(w[2], w[1]);
-    w[5] = cmul(w[4], w[1]);
-    w[6] = cmul(w[4], w[2]);
-    w[7] = cmul(w[4], w[3]);
-  } else {
-    load_tw<R>(w, base);
-  }
-}
-
-template <int N, int E, int NS, int R, typename C>
-__device__ __forceinline__ void row_compute(C (&v)[E], const C* __restrict__ tw, int t) {
-  constexpr int TH = N / E;
-  constexpr int Q = E / R;
-#pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    if constexpr (NS > 1) {
-      const int j = t + TH * q;
-      const int p = j % NS;
-      C w[R + 1];
-      if constexpr (sizeof(C) == 8)
-        derive_tw<R>(w, tw + p * even_up<R>());
-      else
-        load_tw<R>(w, tw + p * even_up<R>());
-#pragma unroll
-      for (int r = 1; r < R; ++r) v[q * R + r] = cmul(v[q * R + r], w[r]);
-    }
-    dft<R>(&v[q * R]);
-  }
-}
-
-// After stage (NS, R): outputs go to smem in Stockham order (swizzled).
-template <int N, int E, int NS, int R, typename C>
-__device__ __forceinline__ void row_write(const C (&v)[E], C* buf, int t) {
-  constexpr int TH = N / E;
-  constexpr int Q = E / R;
-#pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    const int j = t + TH * q;
-    if constexpr (NS == 1 && (R % 2 == 0) && sizeof(C) == 8) {
-      // R consecutive outputs j*R + r: store as 16-byte pairs
-#pragma unroll
-      for (int r = 0; r < R; r += 2) {
-        const int i = swz(j * R + r);
-        *reinterpret_cast<float4*>(buf + i) =
-            make_float4(v[q * R + r].x, v[q * R + r].y, v[q * R + r + 1].x, v[q * R + r + 1].y);
-      }
-    } else {
-      const int p = j % NS;
-      const int base = (j - p) * R + p;
-#pragma unroll
-      for (int r = 0; r < R; ++r) buf[swz(base + r * NS)] = v[q * R + r];
-    }
-  }
-}
-
-// Before a stage of radix R: v[q*R + r] = element j_q + r*N/R.
-template <int N, int E, int R, typename C>
-__device__ __forceinline__ void row_read(C (&v)[E], const C* buf, int t) {
-  constexpr int TH = N / E;
-  constexpr int Q = E / R;
-#pragma unroll
-  for (int q = 0; q < Q; ++q)
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[q * R + r] = buf[swz(t + TH * q + r * (N / R))];
-}
 
 // Double-buffered exchanges (bufs = 2 regions of PITCH elements).
 template <int N, int E, int NS, int OFF, int BUF, int PITCH, typename C, int R, int... Rest>
@@ -410,143 +289,52 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_tma_kernel(const Pa
   }
 }
 
-// ---- strided pencils (the y / z axes of fft2D / fft3D, spectral product) -----
-// A CTA transforms W adjacent columns of a stride-es axis of length N: thread
-// (x, t) holds elements t + TH*m of column x in registers, global accesses are
-// W-column row segments, and the exchanges use a column-interleaved layout
-// [i][x] (x fastest), which keeps every Stockham access pattern free of bank
-// conflicts.  With F_SPEC the kernel multiplies the spectrum by filter[k*S +
-// column], conjugates, and runs the same stages again straight from
-// registers (the output index set of a transform is the input index set of
-// the next), giving the forward z DFT, product and first inverse axis of the
-// spectral convolution in one pass.
-template <int N, int E, int NS, int R, int W, typename C>
-__device__ __forceinline__ void str_write(const C (&v)[E], C* buf, int t, int x) {
-  constexpr int TH = N / E;
-  constexpr int Q = E / R;
-#pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    const int j = t + TH * q;
-    const int p = j % NS;
-    const int base = (j - p) * R + p;
-#pragma unroll
-    for (int r = 0; r < R; ++r) buf[(base + r * NS) * W + x] = v[q * R + r];
-  }
-}
-template <int N, int E, int R, int W, typename C>
-__device__ __forceinline__ void str_read(C (&v)[E], const C* buf, int t, int x) {
-  constexpr int TH = N / E;
-  constexpr int Q = E / R;
-#pragma unroll
-  for (int q = 0; q < Q; ++q)
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[q * R + r] = buf[(t + TH * q + r * (N / R)) * W + x];
-}
-template <int N, int E, int NS, int OFF, int W, typename C, int R, int... Rest>
-__device__ __forceinline__ void str_stages(C (&v)[E], C* b, const C* __restrict__ tw, int t, int x,
-                                           RL<R, Rest...>) {
-  row_compute<N, E, NS, R>(v, tw + OFF, t);
-  if constexpr (sizeof...(Rest) > 0) {
-    str_write<N, E, NS, R, W>(v, b, t, x);
-    __syncthreads();
-    constexpr int R2 = rl_first(RL<Rest...>{});
-    str_read<N, E, R2, W>(v, b, t, x);
-    __syncthreads();
-    str_stages<N, E, NS * R, OFF + NS * even_up<R>(), W>(v, b, tw, t, x, RL<Rest...>{});
-  }
-}
-
-template <typename T, int N, int W, int MINB, int... Rs>
-__global__ void __launch_bounds__(W*(N / 16), MINB) strfft_kernel(const PassDesc d) {
-  using C = typename CxT<T>::type;
-  constexpr int E = 16;
-  constexpr int TH = N / E;
-  constexpr int R0 = rl_first(RL<Rs...>{});
-  constexpr int RZ = rl_last(RL<Rs...>{});
-  static_assert(R0 == 16 || E % R0 == 0, "radix");
+// Passes with a second in-register transform get more registers per thread.
+template <typename T, int N, int W, int MINB, uint32_t OPS, int... Rs>
+__global__ void __launch_bounds__(W*(N / 16), ((OPS & (F_SPEC | F_BLUE)) && MINB > 2) ? 2 : MINB)
+    strfft_kernel(const PassDesc d) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* b = reinterpret_cast<C*>(smem_raw);
-  const int x = threadIdx.x % W;
-  const int t = threadIdx.x / W;
-  const int64_t tiles = (d.ncols + W - 1) / W;
-  const int64_t bq = int64_t(blockIdx.x) / tiles;
-  const int64_t c0 = (int64_t(blockIdx.x) - bq * tiles) * W;
-  const int64_t b_hi = bq / d.nb_lo;
-  const int64_t b_lo = bq - b_hi * d.nb_lo;
-  const int64_t col = c0 + x;
-  const bool ok = col < d.ncols;
-  const uint32_t fl = d.flags;
-  const C* __restrict__ in = static_cast<const C*>(d.in) + b_lo * d.in_bs + b_hi * d.in_bs2 + col * d.in_cs;
-  C* __restrict__ out = static_cast<C*>(d.out) + b_lo * d.out_bs + b_hi * d.out_bs2 + col * d.out_cs;
-  const C* __restrict__ tw = static_cast<const C*>(d.tw);
-  const bool stream_in = (fl & F_L2_IN_FIRST) != 0;
-  const uint64_t ipol = stream_in ? l2_policy_first() : 0;
-  C v[E];
-#pragma unroll
-  for (int q = 0; q < E / R0; ++q)
-#pragma unroll
-    for (int r = 0; r < R0; ++r) {
-      C e = cmake<C>(T(0), T(0));
-      if (ok) {
-        const C* a = in + int64_t(t + TH * (q + r * (E / R0))) * d.in_es;
-        e = stream_in ? ld_l2hint(a, ipol) : *a;
-      }
-      if (fl & F_CONJ_IN) e.y = -e.y;
-      v[q * R0 + r] = e;
-    }
-  str_stages<N, E, 1, 0, W>(v, b, tw, t, x, RL<Rs...>{});
-  if (fl & F_SPEC) {
-    // v[q*RZ + r] holds X[k], k = t + TH*(q + r*E/RZ); the next transform's
-    // first stage wants x[t + TH*(q' + r'*E/R0)] in v[q'*R0 + r']
-    const C* __restrict__ filt = static_cast<const C*>(d.filter);
-    C u[E];
-#pragma unroll
-    for (int q = 0; q < E / RZ; ++q)
-#pragma unroll
-      for (int r = 0; r < RZ; ++r) {
-        const int m = q + r * (E / RZ);
-        const int k = t + TH * m;
-        const C h = ok ? filt[int64_t(k) * d.lout_es + col * d.lout_cs] : cmake<C>(T(0), T(0));
-        const C z = cconj(cmul(v[q * RZ + r], h));
-        // slot of m in the first-stage ordering: m = q' + r' * (E / R0)
-        u[(m % (E / R0)) * R0 + m / (E / R0)] = z;
-      }
-#pragma unroll
-    for (int i = 0; i < E; ++i) v[i] = u[i];
-    __syncthreads();
-    str_stages<N, E, 1, 0, W>(v, b, tw, t, x, RL<Rs...>{});
-  }
-  if (!ok) return;
-  const T s = T(d.scale);
-  const bool keep = (fl & F_L2_OUT_LAST) != 0;
-  const uint64_t pol = keep ? l2_policy_last() : 0;
-#pragma unroll
-  for (int q = 0; q < E / RZ; ++q)
-#pragma unroll
-    for (int r = 0; r < RZ; ++r) {
-      C e = v[q * RZ + r];
-      if (fl & F_SCALE) e = cscale(e, s);
-      if (fl & F_CONJ_OUT) e.y = -e.y;
-      C* o = out + int64_t(t + TH * (q + r * (E / RZ))) * d.out_es;
-      if (keep)
-        st_l2hint(o, e, pol);
-      else
-        *o = e;
-    }
+  str_tile<T, N, W, OPS, Rs...>(d, int64_t(blockIdx.x), smem_raw);
 }
 
 template <typename T, int N, int W, int MINB, int... Rs>
 struct StrCfg {
   static constexpr int threads = W * (N / 16);
   static size_t smem() { return size_t(N) * W * sizeof(typename CxT<T>::type); }
+  template <uint32_t OPS>
+  static cudaError_t prep1() {
+    return cudaFuncSetAttribute(strfft_kernel<T, N, W, MINB, OPS, Rs...>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem()));
+  }
   static cudaError_t prepare() {
-    return cudaFuncSetAttribute(strfft_kernel<T, N, W, MINB, Rs...>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(smem()));
+    cudaError_t e = prep1<SO_PLAIN>();
+    if (e == cudaSuccess) e = prep1<SO_TW4>();
+    if (e == cudaSuccess) e = prep1<SO_TW4B>();
+    if (e == cudaSuccess) e = prep1<SO_BP1>();
+    if (e == cudaSuccess) e = prep1<SO_FILT>();
+    if (e == cudaSuccess) e = prep1<SO_COUT>();
+    if (e == cudaSuccess) e = prep1<SO_SPEC>();
+    if (e == cudaSuccess) e = prep1<SO_BLUE>();
+    return e;
+  }
+  template <uint32_t OPS>
+  static cudaError_t go(const PassDesc& d, cudaStream_t s) {
+    const int64_t tiles = (d.ncols + W - 1) / W;
+    strfft_kernel<T, N, W, MINB, OPS, Rs...><<<unsigned(tiles * d.nbatch), threads, smem(), s>>>(d);
+    return cudaGetLastError();
   }
   static cudaError_t launch(const PassDesc& d, cudaStream_t s) {
-    const int64_t tiles = (d.ncols + W - 1) / W;
-    strfft_kernel<T, N, W, MINB, Rs...><<<unsigned(tiles * d.nbatch), threads, smem(), s>>>(d);
-    return cudaGetLastError();
+    switch (d.flags & kStrOpMask) {
+      case SO_PLAIN: return go<SO_PLAIN>(d, s);
+      case SO_TW4: return go<SO_TW4>(d, s);
+      case SO_TW4B: return go<SO_TW4B>(d, s);
+      case SO_BP1: return go<SO_BP1>(d, s);
+      case SO_FILT: return go<SO_FILT>(d, s);
+      case SO_COUT: return go<SO_COUT>(d, s);
+      case SO_SPEC: return go<SO_SPEC>(d, s);
+      case SO_BLUE: return go<SO_BLUE>(d, s);
+      default: return cudaErrorInvalidValue;
+    }
   }
 };
 

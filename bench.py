@@ -116,6 +116,12 @@ WORKLOADS = {
                             desc="fft innermost, Complex Float 65536x1000 (8*5*5*5), N(0,1)"),
     "many_4096x1009": dict(kind="many", shape=(4096, 1009), dtype="c32", mode="forward",
                            desc="fft innermost, Complex Float 4096x1009 (Bluestein), N(0,1)"),
+    "fft3d_256": dict(kind="full", shape=(256, 256, 256), dtype="c32", mode="forward",
+                      desc="fft3D Forward, Complex Float 256^3, N(0,1)"),
+    "many_2048x65536": dict(kind="many", shape=(2048, 65536), dtype="c32", mode="forward",
+                            desc="fft innermost, Complex Float 2048x65536 (four-step), N(0,1)"),
+    "many_1024x65521": dict(kind="many", shape=(1024, 65521), dtype="c32", mode="forward",
+                            desc="fft innermost, Complex Float 1024x65521 (four-pass Bluestein), N(0,1)"),
     "fft1d_1024_c64": dict(kind="full", shape=(1024,), dtype="c64", mode="forward",
                            desc="fft1D Forward, Complex Double N=1024, U[-1,1]"),
     "specconv_8x256": dict(kind="specconv", shape=(8, 256, 256, 256), dtype="c32",
