@@ -13,6 +13,8 @@ constexpr int kMaxStages = 16;
 // Value a kernel writes into a plan's device status word when a bounded wait
 // gives up (equals GBFFT_ERR_TIMEOUT of the C ABI).
 constexpr int GBFFT_ERR_TIMEOUT_DEVICE = 6;
+// ... when a kernel's own alignment check fails (GBFFT_ERR_INTERNAL).
+constexpr int GBFFT_ERR_INTERNAL_DEVICE = 7;
 
 // Largest transform length one CTA computes in shared memory (two ping-pong
 // buffers of one column each); longer axes are split four-step.
@@ -100,6 +102,10 @@ size_t pass_smem_bytes(const PassDesc& d, bool is_double);
 int pass_grid(const PassDesc& d);
 
 // Launch one pencil pass on `stream`; returns a cudaError_t.
+// Name of the __global__ function launch_pass runs for d (a 16-byte aligned
+// input assumed).
+const char* pass_kernel_name(const PassDesc& d, bool is_double);
+const char* str_kernel_name(const PassDesc& d, bool is_double);
 cudaError_t launch_pass(const PassDesc& d, bool is_double, cudaStream_t stream);
 
 // Prepare kernel attributes (max dynamic shared memory); idempotent.

@@ -42,6 +42,21 @@ cudaError_t prepare_kernels() {
                               227 * 1024);
 }
 
+const char* pass_kernel_name(const PassDesc& d, bool dbl) {
+  switch (d.kernel) {
+    case K_ROW:
+      if (d.row_variant & 1) return "rowfft1_kernel";
+      return (d.use_tma && d.in_cs == d.n && d.out_cs == d.n) ? "rowfft_tma_kernel" : "rowfft_kernel";
+    case K_COL4096:
+      return d.col_variant >= 8 ? "colfft4096_r16_kernel"
+           : d.col_variant >= 4 ? "colfft4096_push_kernel"
+                                : "colfft4096_kernel";
+    case K_ROW_TC: return "rowfft_tc_kernel";
+    case K_STRIDED: return str_kernel_name(d, dbl);
+    default: return "pencil_kernel";
+  }
+}
+
 cudaError_t launch_pass(const PassDesc& d, bool is_double, cudaStream_t stream) {
   if (d.kernel == K_ROW) return launch_row(d, is_double, stream);
   if (d.kernel == K_COL4096) return launch_col4096(d, is_double, stream);

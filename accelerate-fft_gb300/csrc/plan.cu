@@ -1012,4 +1012,11 @@ int gbfft_plan_describe(const gbfft_plan* plan, char* buf, size_t cap) {
   return GBFFT_OK;
 }
 
+int gbfft_plan_pass_kernel(const gbfft_plan* plan, int pass, char* buf, size_t cap) {
+  if (!plan) return GBFFT_ERR_NULL_PLAN;
+  if (!buf || cap == 0 || pass < 0 || size_t(pass) >= plan->passes.size()) return GBFFT_ERR_INVALID_ARG;
+  std::snprintf(buf, cap, "%s", gbfft::pass_kernel_name(plan->passes[size_t(pass)].d, plan->dbl));
+  return GBFFT_OK;
+}
+
 }  // extern "C"

@@ -27,6 +27,7 @@
 #include "butterflies.cuh"
 #include "gbfft_internal.h"
 #include "strided_tile.cuh"
+#include "tma.cuh"
 
 namespace gbfft {
 
@@ -158,46 +159,6 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft1_kernel(const PassD
 }
 
 // ---- TMA-fed persistent variant (Complex Float) ----------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void fence_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-constexpr uint32_t kWaitLimit = 1u << 22;  // try_wait polls before giving up
-
-// Bounded wait; returns false (and records a timeout) if it gave up.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
-  for (uint32_t it = 0; it < kWaitLimit; ++it)
-    if (mbar_try_wait(bar, parity)) return true;
-  if (status) atomicExch(status, GBFFT_ERR_TIMEOUT_DEVICE);
-  return false;
-}
-
 template <int N, int E, int ROWS, int MINB, int... Rs>
 __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_tma_kernel(const PassDesc d) {
   using C = float2;
@@ -288,66 +249,6 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_tma_kernel(const Pa
     }
   }
 }
-
-// Passes with a second in-register transform get more registers per thread.
-template <typename T, int N, int W, int MINB, uint32_t OPS, int... Rs>
-__global__ void __launch_bounds__(W*(N / 16), ((OPS & (F_SPEC | F_BLUE)) && MINB > 2) ? 2 : MINB)
-    strfft_kernel(const PassDesc d) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  str_tile<T, N, W, OPS, Rs...>(d, int64_t(blockIdx.x), smem_raw);
-}
-
-template <typename T, int N, int W, int MINB, int... Rs>
-struct StrCfg {
-  static constexpr int threads = W * (N / 16);
-  static size_t smem() { return size_t(N) * W * sizeof(typename CxT<T>::type); }
-  template <uint32_t OPS>
-  static cudaError_t prep1() {
-    return cudaFuncSetAttribute(strfft_kernel<T, N, W, MINB, OPS, Rs...>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem()));
-  }
-  static cudaError_t prepare() {
-    cudaError_t e = prep1<SO_PLAIN>();
-    if (e == cudaSuccess) e = prep1<SO_TW4>();
-    if (e == cudaSuccess) e = prep1<SO_TW4B>();
-    if (e == cudaSuccess) e = prep1<SO_BP1>();
-    if (e == cudaSuccess) e = prep1<SO_FILT>();
-    if (e == cudaSuccess) e = prep1<SO_COUT>();
-    if (e == cudaSuccess) e = prep1<SO_SPEC>();
-    if (e == cudaSuccess) e = prep1<SO_BLUE>();
-    return e;
-  }
-  template <uint32_t OPS>
-  static cudaError_t go(const PassDesc& d, cudaStream_t s) {
-    const int64_t tiles = (d.ncols + W - 1) / W;
-    strfft_kernel<T, N, W, MINB, OPS, Rs...><<<unsigned(tiles * d.nbatch), threads, smem(), s>>>(d);
-    return cudaGetLastError();
-  }
-  static cudaError_t launch(const PassDesc& d, cudaStream_t s) {
-    switch (d.flags & kStrOpMask) {
-      case SO_PLAIN: return go<SO_PLAIN>(d, s);
-      case SO_TW4: return go<SO_TW4>(d, s);
-      case SO_TW4B: return go<SO_TW4B>(d, s);
-      case SO_BP1: return go<SO_BP1>(d, s);
-      case SO_FILT: return go<SO_FILT>(d, s);
-      case SO_COUT: return go<SO_COUT>(d, s);
-      case SO_SPEC: return go<SO_SPEC>(d, s);
-      case SO_BLUE: return go<SO_BLUE>(d, s);
-      default: return cudaErrorInvalidValue;
-    }
-  }
-};
-
-// (type, N, W, min CTAs per SM, radices = factor_device(N))
-#define GBFFT_STR_TABLE(X)                 \
-  X(float, 256, 16, 3, 16, 16)             \
-  X(float, 512, 16, 2, 16, 16, 2)          \
-  X(float, 1024, 16, 1, 16, 16, 4)         \
-  X(float, 128, 16, 4, 16, 8)              \
-  X(float, 64, 16, 4, 16, 4)               \
-  X(double, 256, 8, 2, 16, 16)             \
-  X(double, 512, 8, 1, 16, 16, 2)          \
-  X(double, 1024, 8, 1, 16, 16, 4)
 
 // ---- split-FP16 tensor-core variant (Complex Float) --------------------------
 // Every radix-16 stage runs as a GEMM on the 5th-generation tensor cores:
@@ -703,33 +604,6 @@ cudaError_t prepare_row_kernels() {
   GBFFT_ROW_TABLE(X)
 #undef X
   return e;
-}
-
-bool str_kernel_available(int n, bool dbl) {
-#define X(T, N, W, MINB, ...) \
-  if (n == N && dbl == (sizeof(T) == 8)) return true;
-  GBFFT_STR_TABLE(X)
-#undef X
-  return false;
-}
-
-int str_kernel_width(bool dbl) { return dbl ? 8 : 16; }
-
-cudaError_t prepare_str_kernels() {
-  cudaError_t e = cudaSuccess;
-#define X(T, N, W, MINB, ...) \
-  if (e == cudaSuccess) e = StrCfg<T, N, W, MINB, __VA_ARGS__>::prepare();
-  GBFFT_STR_TABLE(X)
-#undef X
-  return e;
-}
-
-cudaError_t launch_str(const PassDesc& d, bool dbl, cudaStream_t s) {
-#define X(T, N, W, MINB, ...) \
-  if (d.n == N && dbl == (sizeof(T) == 8)) return StrCfg<T, N, W, MINB, __VA_ARGS__>::launch(d, s);
-  GBFFT_STR_TABLE(X)
-#undef X
-  return cudaErrorInvalidValue;
 }
 
 bool row_tc_available(int n) {

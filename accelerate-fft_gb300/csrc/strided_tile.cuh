@@ -193,52 +193,58 @@ enum StrOps : uint32_t {
 constexpr uint32_t kStrOpMask = F_TW4 | F_TW4_BATCH | F_PAD_IN | F_CHIRP_IN | F_FILTER_OUT | F_CHIRP_OUT |
                                 F_TRUNC_OUT | F_SPEC | F_BLUE;
 
-// One tile (W columns) of a strided pass.  OPS selects the fused operations:
-// conjugate, Bluestein chirp and zero padding on load; spectral product or
-// in-kernel Bluestein (second transform from registers); four-step twiddle,
-// filter, chirp, truncation, scale and conjugate on store.  Stores go
-// straight from registers when consecutive columns are adjacent in memory
-// (out_cs == 1); otherwise (the transposed store of a four-step first half)
-// they go through shared memory so that a warp writes consecutive k.
-template <typename T, int N, int W, uint32_t OPS, int... Rs>
-__device__ __forceinline__ void str_tile(const PassDesc& d, int64_t tile, unsigned char* smem_raw) {
+// Position of one thread's column inside a tile of a strided pass.
+struct StrCtx {
+  int x, t;                  // column within the tile, butterfly row
+  int64_t c0, b_lo, b_hi;    // first column of the tile, batch indices
+  int64_t col;               // this thread's column
+  bool ok;                   // col < ncols
+};
+
+template <int N, int W>
+__device__ __forceinline__ StrCtx str_ctx(const PassDesc& d, int64_t tile) {
+  StrCtx c;
+  c.x = threadIdx.x % W;
+  c.t = threadIdx.x / W;
+  const int64_t tiles = (d.ncols + W - 1) / W;
+  const int64_t bq = tile / tiles;
+  c.c0 = (tile - bq * tiles) * W;
+  c.b_hi = bq / d.nb_lo;
+  c.b_lo = bq - c.b_hi * d.nb_lo;
+  c.col = c.c0 + c.x;
+  c.ok = c.col < d.ncols;
+  return c;
+}
+
+// Loads of one tile straight from global memory: thread (x, t) reads
+// elements t + TH*m of its column, with conjugation, Bluestein chirp and
+// zero padding as OPS asks.
+template <typename T, int N, int W, uint32_t OPS, int R0>
+__device__ __forceinline__ void str_load_global(const PassDesc& d, const StrCtx& c,
+                                                typename CxT<T>::type (&v)[16]) {
   using C = typename CxT<T>::type;
   constexpr int E = 16;
   constexpr int TH = N / E;
-  constexpr int R0 = rl_first(RL<Rs...>{});
-  constexpr int RZ = rl_last(RL<Rs...>{});
-  C* b = reinterpret_cast<C*>(smem_raw);
-  const int x = threadIdx.x % W;
-  const int t = threadIdx.x / W;
-  const int64_t tiles = (d.ncols + W - 1) / W;
-  const int64_t bq = tile / tiles;
-  const int64_t c0 = (tile - bq * tiles) * W;
-  const int64_t b_hi = bq / d.nb_lo;
-  const int64_t b_lo = bq - b_hi * d.nb_lo;
-  const int64_t col = c0 + x;
-  const bool ok = col < d.ncols;
   const uint32_t fl = d.flags;
   const T csign_in = (fl & F_CONJ_IN) ? T(-1) : T(1);
-  const C* __restrict__ tw = static_cast<const C*>(d.tw);
   const C* __restrict__ chirp = static_cast<const C*>(d.chirp);
-  const C* __restrict__ filt = static_cast<const C*>(d.filter);
   const bool stream_in = (fl & F_L2_IN_FIRST) != 0;
   const uint64_t ipol = stream_in ? l2_policy_first() : 0;
   const int64_t ies = d.in_es;
-  const C* __restrict__ in = static_cast<const C*>(d.in) + b_lo * d.in_bs + b_hi * d.in_bs2 +
-                             (ok ? (d.col_in_off ? d.col_in_off[col] : col * d.in_cs) : 0) + int64_t(t) * ies;
-  C v[E];
+  const C* __restrict__ in = static_cast<const C*>(d.in) + c.b_lo * d.in_bs + c.b_hi * d.in_bs2 +
+                             (c.ok ? (d.col_in_off ? d.col_in_off[c.col] : c.col * d.in_cs) : 0) +
+                             int64_t(c.t) * ies;
 #pragma unroll
   for (int q = 0; q < E / R0; ++q)
 #pragma unroll
     for (int r = 0; r < R0; ++r) {
       const int m = q + r * (E / R0);
-      const int i = t + TH * m;
+      const int i = c.t + TH * m;
       C e = cmake<C>(T(0), T(0));
-      bool valid = ok;
+      bool valid = c.ok;
       int64_t l = 0;
       if constexpr ((OPS & (F_PAD_IN | F_CHIRP_IN)) != 0) {
-        l = int64_t(i) * d.lin_es + col * d.lin_cs;
+        l = int64_t(i) * d.lin_es + c.col * d.lin_cs;
         if ((OPS & F_PAD_IN) && l >= d.n_in) valid = false;
       }
       if (valid) {
@@ -249,6 +255,28 @@ __device__ __forceinline__ void str_tile(const PassDesc& d, int64_t tile, unsign
       }
       v[q * R0 + r] = e;
     }
+}
+
+// Everything of a tile after its loads: the stages, the optional second
+// transform (spectral product or in-kernel Bluestein), the store-side
+// operations and the stores.  b is the tile's exchange buffer (N*W
+// elements); every thread must be done reading its inputs from b, if they
+// came from there, before the call.
+template <typename T, int N, int W, uint32_t OPS, int... Rs>
+__device__ __forceinline__ void str_finish(const PassDesc& d, const StrCtx& c,
+                                           typename CxT<T>::type (&v)[16], typename CxT<T>::type* b) {
+  using C = typename CxT<T>::type;
+  constexpr int E = 16;
+  constexpr int TH = N / E;
+  constexpr int R0 = rl_first(RL<Rs...>{});
+  constexpr int RZ = rl_last(RL<Rs...>{});
+  const int x = c.x, t = c.t;
+  const int64_t col = c.col, c0 = c.c0;
+  const bool ok = c.ok;
+  const uint32_t fl = d.flags;
+  const C* __restrict__ tw = static_cast<const C*>(d.tw);
+  const C* __restrict__ chirp = static_cast<const C*>(d.chirp);
+  const C* __restrict__ filt = static_cast<const C*>(d.filter);
   str_stages<N, E, 1, 0, W>(v, b, tw, t, x, RL<Rs...>{});
   if constexpr ((OPS & (F_SPEC | F_BLUE)) != 0) {
     // v[q*RZ + r] holds X[k], k = t + TH*(q + r*E/RZ); the next transform's
@@ -282,7 +310,8 @@ __device__ __forceinline__ void str_tile(const PassDesc& d, int64_t tile, unsign
   const C* __restrict__ tw4_hi = static_cast<const C*>(d.tw4_hi);
   const int tw4_shift = d.tw4_shift;
   const int64_t tw4_mask = (int64_t(1) << tw4_shift) - 1;
-  C* __restrict__ out = static_cast<C*>(d.out) + b_lo * d.out_bs + b_hi * d.out_bs2;
+  const int64_t b_lo = c.b_lo;
+  C* __restrict__ out = static_cast<C*>(d.out) + c.b_lo * d.out_bs + c.b_hi * d.out_bs2;
   const int64_t oes = d.out_es;
   // post-operations of output k of column cl; returns false when truncated
   auto post = [&](C& e, int k, int64_t cl) -> bool {
@@ -327,10 +356,10 @@ __device__ __forceinline__ void str_tile(const PassDesc& d, int64_t tile, unsign
     __syncthreads();
 #pragma unroll 4
     for (int f = threadIdx.x; f < N * W; f += W * TH) {
-      const int c = f / N, k = f % N;
-      const int64_t cl = c0 + c;
+      const int cc = f / N, k = f % N;
+      const int64_t cl = c0 + cc;
       if (cl >= d.ncols) continue;
-      C e = b[k * W + c];
+      C e = b[k * W + cc];
       if (!post(e, k, cl)) continue;
       const int64_t cb = d.col_out_off ? d.col_out_off[cl] : cl * d.out_cs;
       C* o = out + cb + int64_t(k) * oes;
@@ -340,6 +369,23 @@ __device__ __forceinline__ void str_tile(const PassDesc& d, int64_t tile, unsign
         *o = e;
     }
   }
+}
+
+// One tile (W columns) of a strided pass.  OPS selects the fused operations:
+// conjugate, Bluestein chirp and zero padding on load; spectral product or
+// in-kernel Bluestein (second transform from registers); four-step twiddle,
+// filter, chirp, truncation, scale and conjugate on store.  Stores go
+// straight from registers when consecutive columns are adjacent in memory
+// (out_cs == 1); otherwise (the transposed store of a four-step first half)
+// they go through shared memory so that a warp writes consecutive k.
+template <typename T, int N, int W, uint32_t OPS, int... Rs>
+__device__ __forceinline__ void str_tile(const PassDesc& d, int64_t tile, unsigned char* smem_raw) {
+  using C = typename CxT<T>::type;
+  constexpr int R0 = rl_first(RL<Rs...>{});
+  const StrCtx c = str_ctx<N, W>(d, tile);
+  C v[16];
+  str_load_global<T, N, W, OPS, R0>(d, c, v);
+  str_finish<T, N, W, OPS, Rs...>(d, c, v, reinterpret_cast<C*>(smem_raw));
 }
 
 // Calls the instantiation for the pass's fused-operation set.

@@ -93,6 +93,15 @@ class Plan:
         L.check(L.lib().gbfft_plan_describe(self.handle, buf, 4096))
         return buf.value.decode()
 
+    def pass_kernels(self):
+        """CUDA kernel name of each launch of one exec, in order."""
+        out = []
+        for i in range(self.info["launches"]):
+            buf = ctypes.create_string_buffer(128)
+            L.check(L.lib().gbfft_plan_pass_kernel(self.handle, i, buf, 128))
+            out.append(buf.value.decode())
+        return out
+
     def close(self):
         if getattr(self, "handle", None):
             L.lib().gbfft_plan_destroy(self.handle)

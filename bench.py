@@ -238,6 +238,7 @@ def run_gbfft(args, wl):
     plan = gbfft.Plan(shape, kind=wl["kind"], dtype=dtype, precision=args.precision)
     info = plan.info
     npass = info["launches"]
+    kernels = plan.pass_kernels()
     mode = gbfft.mode_code(wl["mode"])
     stream = torch.cuda.current_stream(dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
@@ -292,6 +293,7 @@ def run_gbfft(args, wl):
 
     # accuracy of one result vs FP64 (numpy pocketfft), outside the timed region
     rel_err = None
+    ref = None
     if rank == 0 and not args.no_check:
         one_step()
         torch.cuda.synchronize()
@@ -300,6 +302,41 @@ def run_gbfft(args, wl):
         axes = tuple(range(len(shape))) if wl["kind"] == "full" else (-1,)
         ref = np.fft.fftn(xx, axes=axes) if wl["mode"] == "forward" else np.fft.ifftn(xx, axes=axes)
         rel_err = float(np.linalg.norm(yy - ref) / np.linalg.norm(ref))
+
+    # the other precision of the same transform (split-FP16 tensor-core rows vs
+    # plain FP32), timed the same way, with its own error vs FP64
+    other_prec = None
+    if rank == 0 and wl["dtype"] == "c32" and not args.no_compare:
+        other = "split_fp16" if args.precision == "plain" else "plain"
+        try:
+            p2 = gbfft.Plan(shape, kind=wl["kind"], dtype=dtype, precision=other)
+        except Exception as exc:  # the planner rejects shapes it has no kernel for
+            other_prec = {"precision": other, "unavailable": str(exc)}
+        else:
+            for _ in range(max(3, args.warmup)):
+                L.check(lib.gbfft_exec(p2.handle, mode, ctypes.c_void_p(x.data_ptr()),
+                                       ctypes.c_void_p(y.data_ptr()), sp))
+            ts = []
+            for k in range(args.steps):
+                flush.fill_(float(k))
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                L.check(lib.gbfft_exec(p2.handle, mode, ctypes.c_void_p(x.data_ptr()),
+                                       ctypes.c_void_p(y.data_ptr()), sp))
+                b.record(stream)
+                torch.cuda.synchronize()
+                ts.append(a.elapsed_time(b))
+            ms2 = statistics.mean(ts)
+            err2 = None
+            if ref is not None:
+                yy2 = y.cpu().numpy().astype(np.complex128)
+                err2 = float(np.linalg.norm(yy2 - ref) / np.linalg.norm(ref))
+            other_prec = {"precision": other, "ms_per_step": ms2,
+                          "value": fl * world / (ms2 * 1e-3) / 1e9, "unit": "GFLOP/s",
+                          "rel_err_vs_fp64": err2, "speedup_of_split_fp16_over_fp32":
+                              (ms / ms2) if other == "split_fp16" else (ms2 / ms),
+                          "kernels": p2.pass_kernels()}
+            p2.close()
 
     # end to end through the C ABI with host buffers (pinned), H2D + exec + D2H
     hx = x_cpu.pin_memory()
@@ -352,13 +389,13 @@ def run_gbfft(args, wl):
                        "plan": plan.describe(), "parallelism": "replicas" if world > 1 else "single"},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                          "frac": ach / peak, "traffic": None, "peak_source": peak_kind,
-                         "kernel": "pass %d of %d (%s)" % (dom, npass, "pencil_kernel<float>"
-                                                           if elem == 8 else "pencil_kernel<double>"),
+                         "kernel": "pass %d of %d (%s)" % (dom, npass, kernels[dom] if npass else "-"),
                          "bytes_alg_per_launch": bytes_pass,
                          "kernel_ms": avg_pass[dom] if npass else None},
-            "roofline_transform": {"achieved": ach_tr, "frac": ach_tr / peak,
+            "roofline_transform": {"achieved": ach_tr, "frac": ach_tr / peak, "kernels": kernels,
                                    "bytes_alg": bytes_pass, "pass_ms": avg_pass},
             "rel_err_vs_fp64": rel_err,
+            "other_precision": other_prec,
             "e2e": {"value": e2e, "unit": "GFLOP/s", "h2d_bytes_per_step": nelem * elem,
                     "d2h_bytes_per_step": nelem * elem, "ms_per_step": statistics.mean(e2e_ms)},
             "gpu_launches": args.steps * npass,
@@ -663,6 +700,8 @@ def main():
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cufft", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip timing the other precision (split-FP16 vs FP32)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -128,6 +128,11 @@ int gbfft_plan_explain(int rank, const int64_t* dims, int kind, int dtype, int p
  * into buf (NUL-terminated, truncated to cap). */
 int gbfft_plan_describe(const gbfft_plan* plan, char* buf, size_t cap);
 
+/* Name of the CUDA kernel that launch `pass` (0-based, in execution order)
+ * of one exec runs, e.g. "colfft4096_r16_kernel"; used to match timings to
+ * profiler launch lists.  No counterpart in the reference. */
+int gbfft_plan_pass_kernel(const gbfft_plan* plan, int pass, char* buf, size_t cap);
+
 /* ---- ragged batch: new beyond the reference API -------------------------
  * `count` independent 1D transforms of uneven lengths over one flat buffer,
  * executed by one persistent launch (the reference can only express this as

@@ -363,3 +363,62 @@ def test_split_fp16_accuracy(gbfft_lib, shape, kind):
             assert np.all(y == 0)
         else:
             assert rel_l2(y, ref) < 2e-6, scale
+
+
+# ---- strided passes: tensor-copy-fed persistent kernel vs direct loads ------
+TMA_CASES = [((256, 48), "full", np.complex64), ((3, 256, 32), "full", np.complex64),
+             ((2, 65536, 16), "full", np.complex64), ((256, 256, 16), "full", np.complex128),
+             ((4, 65536), "many", np.complex64), ((8, 65521), "many", np.complex64),
+             ((64, 256, 64), "full", np.complex64)]
+
+
+@pytest.mark.parametrize("shape,kind,dt", TMA_CASES)
+def test_strided_tensor_copy_kernel(gbfft_lib, monkeypatch, shape, kind, dt):
+    """Each layout runs once with the tensor-copy kernel (at least one pass
+    must use it) and once with it disabled; both must match FP64 and agree."""
+    g = gbfft_lib
+    from gbfft import _lib as L
+    rng = np.random.default_rng(2024)
+    x = uniform_complex(rng, shape, dt)
+    tdt = torch.complex64 if dt == np.complex64 else torch.complex128
+    name = ("fft3D" if len(shape) == 3 else "fft2D") if kind == "full" else "fft"
+    outs = {}
+    for disable in ("", "tma"):
+        monkeypatch.setenv("GBFFT_DISABLE", disable)
+        plan = g.Plan(shape, kind=kind, dtype=tdt)
+        kernels = plan.pass_kernels()
+        if disable == "":
+            assert "strfft_tma_kernel" in kernels, (shape, kernels, plan.describe())
+        else:
+            assert "strfft_tma_kernel" not in kernels
+        for mode in MODES:
+            y = plan(mode, torch.from_numpy(x).cuda()).cpu().numpy()
+            ref = np_reference(name, MODE_IDX[mode], x)
+            assert rel_l2(y, ref) < tol_fp64(dt, shape if kind == "full" else shape[-1:]), \
+                (shape, mode, disable, plan.describe())
+            outs[(disable, mode)] = y
+        assert L.lib().gbfft_exec_status(plan.handle, None) == 0
+        plan.close()
+    for mode in MODES:
+        assert rel_l2(outs[("", mode)], outs[("tma", mode)]) < 2 * tol_fp64(dt, shape if kind == "full"
+                                                                            else shape[-1:])
+
+
+@pytest.mark.parametrize("shape,kind", [((65536, 16), "full"), ((4, 65536), "many")])
+def test_strided_input_not_16_byte_aligned(gbfft_lib, shape, kind):
+    # the first pass of these plans is a strided four-step half reading the
+    # caller's input; an 8-byte-aligned view cannot be described by a tensor
+    # map (16-byte base), so that launch falls back to direct loads
+    g = gbfft_lib
+    rng = np.random.default_rng(6)
+    n = int(np.prod(shape))
+    base = torch.from_numpy(uniform_complex(rng, (n + 1,), np.complex64)).cuda()
+    view = base[1:].view(*shape)
+    assert view.data_ptr() % 16 == 8
+    plan = g.Plan(shape, kind=kind, dtype=torch.complex64)
+    assert plan.pass_kernels()[0] == "strfft_tma_kernel", plan.describe()
+    out = torch.empty(shape, dtype=torch.complex64, device="cuda")
+    plan.exec_ptr("forward", view.data_ptr(), out.data_ptr())
+    xv = view.cpu().numpy().astype(np.complex128)
+    ref = np.fft.fft2(xv) if kind == "full" else np.fft.fft(xv, axis=-1)
+    assert rel_l2(out.cpu().numpy(), ref) < 2e-6
