@@ -84,7 +84,7 @@ __device__ __noinline__ void ragged_pencil(const PassDesc& d, int64_t tile, unsi
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kRaggedThreads, 2) ragged_kernel(const RaggedArgs a) {
+__global__ void __launch_bounds__(kRaggedThreads, sizeof(T) == 4 ? 3 : 2) ragged_kernel(const RaggedArgs a) {
   using C = typename CxT<T>::type;
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int kDescBytes = (int(sizeof(PassDesc)) + 127) & ~127;

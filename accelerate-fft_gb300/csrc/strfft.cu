@@ -7,8 +7,8 @@
 //    global memory by the threads that transform it.
 //  * strfft_tma_kernel: persistent CTAs.  A tile (W columns x N elements,
 //    one 128-byte row segment per element index) is fetched into shared
-//    memory by one tiled tensor copy (cp.async.bulk.tensor) completing on an
-//    mbarrier, double buffered, so the next tile streams in while the
+//    memory by tiled tensor copies (cp.async.bulk.tensor, one per 256
+//    element indices) completing on an mbarrier, double buffered, so the next tile streams in while the
 //    current one is transformed: the plain kernel waits on its own loads
 //    with nothing else in flight (long-scoreboard stalls dominated its
 //    profile).  The tensor map is encoded on the host for every launch
@@ -38,10 +38,20 @@ __global__ void __launch_bounds__(W*(N / 16), ((OPS & (F_SPEC | F_BLUE)) && MINB
   str_tile<T, N, W, OPS, Rs...>(d, int64_t(blockIdx.x), smem_raw);
 }
 
+// Resident CTAs per SM the tensor-fed kernel can have (shared memory: two
+// tile buffers, alignment slack and barriers, of 227 KB), capped by MINB.
+template <typename T, int N, int W, int MINB, uint32_t OPS>
+constexpr int tma_minb() {
+  constexpr int bytes = 128 + 2 * N * W * int(sizeof(T)) * 2 + 16;
+  constexpr int fit = (227 * 1024) / bytes;
+  constexpr int m = ((OPS & (F_SPEC | F_BLUE)) && MINB > 2) ? 2 : MINB;
+  return fit < 1 ? 1 : (fit < m ? fit : m);
+}
+
 // rank: 2 (one batch), 3 (batch), 4 (batch and outer batch) -- the
 // dimensions of `tmap`, whose box is W columns x N element indices.
 template <typename T, int N, int W, int MINB, uint32_t OPS, int... Rs>
-__global__ void __launch_bounds__(W*(N / 16), ((OPS & (F_SPEC | F_BLUE)) && MINB > 2) ? 2 : MINB)
+__global__ void __launch_bounds__(W*(N / 16), (tma_minb<T, N, W, MINB, OPS>()))
     strfft_tma_kernel(const __grid_constant__ CUtensorMap tmap, const PassDesc d, const int rank) {
   using C = typename CxT<T>::type;
   constexpr int E = 16;
@@ -49,6 +59,8 @@ __global__ void __launch_bounds__(W*(N / 16), ((OPS & (F_SPEC | F_BLUE)) && MINB
   constexpr int TILE = N * W;
   constexpr int K = int(sizeof(C) / 8);  // 8-byte words per element
   constexpr uint32_t kBytes = uint32_t(TILE * sizeof(C));
+  constexpr int NBOX = N > 256 ? N / 256 : 1;  // boxes per tile (a box spans <= 256 indices)
+  constexpr int BOXN = N / NBOX;
   constexpr int R0 = rl_first(RL<Rs...>{});
   // dynamic shared memory only: [pad to 128 B][tile buffer 0][tile buffer 1]
   // [2 mbarriers]; a tensor copy's shared destination must be 128-byte
@@ -74,7 +86,10 @@ __global__ void __launch_bounds__(W*(N / 16), ((OPS & (F_SPEC | F_BLUE)) && MINB
     const int64_t b_lo = bq - b_hi * d.nb_lo;
     mbar_expect_tx(&bars[b], kBytes);
     // c0 is a multiple of W, so the innermost coordinate is 16-byte aligned
-    tma_load_tile(buf0 + b * TILE, &tmap, rank, int(c0 * K), 0, int(b_lo), int(b_hi), &bars[b]);
+#pragma unroll
+    for (int j = 0; j < NBOX; ++j)
+      tma_load_tile(buf0 + b * TILE + j * BOXN * W, &tmap, rank, int(c0 * K), j * BOXN, int(b_lo), int(b_hi),
+                    &bars[b]);
   };
 
   if (threadIdx.x == 0) {
@@ -145,9 +160,10 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 // Rank (2..4) of the tensor map str_tensor_map builds for this pass, or 0
 // when the layout does not fit the tensor-copy rules (strides multiples of
-// 16 bytes, box <= 256 per dimension); checks the layout alone.
+// 16 bytes, box <= 256 per dimension, so N > 256 must be a multiple of
+// 256); checks the layout alone.
 int str_tma_rank(const PassDesc& d, int N, int W, size_t eb) {
-  if (!d.use_tma || d.col_in_off || d.in_cs != 1 || N > 256 || d.ncols < 1) return 0;
+  if (!d.use_tma || d.col_in_off || d.in_cs != 1 || (N > 256 && N % 256) || d.ncols < 1) return 0;
   if (d.flags & (F_PAD_IN | F_CHIRP_IN | F_BLUE)) return 0;
   const int64_t K = int64_t(eb / 8);
   if (int64_t(W) * K > 256) return 0;
@@ -179,7 +195,7 @@ int str_tensor_map(const PassDesc& d, int N, int W, size_t eb, CUtensorMap* map)
   const cuuint64_t dims[4] = {cuuint64_t(d.ncols * K), cuuint64_t(N), cuuint64_t(nb_lo), cuuint64_t(nb_hi)};
   // a size-1 batch dimension below a larger one still needs a valid stride
   const cuuint64_t strides[3] = {es, fits(bs) ? bs : es, bs2};
-  const cuuint32_t box[4] = {cuuint32_t(W * K), cuuint32_t(N), 1, 1};
+  const cuuint32_t box[4] = {cuuint32_t(W * K), cuuint32_t(std::min(N, 256)), 1, 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, cuuint32_t(rank), const_cast<void*>(d.in), dims,
                         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -265,10 +281,10 @@ struct StrCfg {
 // (type, N, W, min CTAs per SM, tensor-fed variant, radices = factor_device(N))
 #define GBFFT_STR_TABLE(X)                 \
   X(float, 256, 16, 3, true, 16, 16)       \
-  X(float, 512, 16, 2, false, 16, 16, 2)   \
+  X(float, 512, 16, 2, true, 16, 16, 2)    \
   X(float, 1024, 16, 1, false, 16, 16, 4)  \
-  X(float, 128, 16, 4, false, 16, 8)       \
-  X(float, 64, 16, 4, false, 16, 4)        \
+  X(float, 128, 16, 6, true, 16, 8)        \
+  X(float, 64, 16, 8, true, 16, 4)         \
   X(double, 256, 8, 2, true, 16, 16)       \
   X(double, 512, 8, 1, false, 16, 16, 2)   \
   X(double, 1024, 8, 1, false, 16, 16, 4)

@@ -347,19 +347,26 @@ __device__ __forceinline__ void str_finish(const PassDesc& d, const StrCtx& c,
           *o = e;
       }
   } else {
-    // transposed store through shared memory: a warp writes consecutive k
+    // transposed store through shared memory: a warp writes consecutive k.
+    // Row k of the staging buffer holds column x at slot x ^ (k mod W) (W is
+    // a power of two), so both the row writes and the column reads of
+    // consecutive k hit distinct banks.
+    static_assert((W & (W - 1)) == 0, "W must be a power of two");
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < E / RZ; ++q)
 #pragma unroll
-      for (int r = 0; r < RZ; ++r) b[(t + TH * (q + r * (E / RZ))) * W + x] = v[q * RZ + r];
+      for (int r = 0; r < RZ; ++r) {
+        const int k = t + TH * (q + r * (E / RZ));
+        b[k * W + (x ^ (k & (W - 1)))] = v[q * RZ + r];
+      }
     __syncthreads();
 #pragma unroll 4
     for (int f = threadIdx.x; f < N * W; f += W * TH) {
       const int cc = f / N, k = f % N;
       const int64_t cl = c0 + cc;
       if (cl >= d.ncols) continue;
-      C e = b[k * W + cc];
+      C e = b[k * W + (cc ^ (k & (W - 1)))];
       if (!post(e, k, cl)) continue;
       const int64_t cb = d.col_out_off ? d.col_out_off[cl] : cl * d.out_cs;
       C* o = out + cb + int64_t(k) * oes;
