@@ -14,9 +14,14 @@
 //            output rows K + 64k'.
 // Every global access is a 128-byte row segment (16 consecutive columns).
 #include <cooperative_groups.h>
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
 
 #include "butterflies.cuh"
 #include "gbfft_internal.h"
+#include "tma.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -63,9 +68,6 @@ __device__ __forceinline__ void apply_powers8(C (&v)[8], const C* __restrict__ w
   v[7] = cmul(v[7], cmul(b4, w3));
 }
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
 // address of the same shared-memory location in CTA `rank` of the cluster
 __device__ __forceinline__ uint32_t mapa_u32(uint32_t addr, uint32_t rank) {
   uint32_t r;
@@ -491,6 +493,127 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
   }
 }
 
+// Persistent form of the radix-16 kernel: each 8-CTA cluster walks a
+// sequence of tiles.  CTA r's 512 input rows (256a + 32r + q, a < 16,
+// q < 32) of W columns arrive by ONE tiled tensor copy (box W x 32 x 16 of
+// the view [a][b][x]) into a load buffer [a][q][x]; as soon as the tile's
+// values are in registers the copy of the cluster's next tile is issued into
+// the same buffer, so HBM reads overlap the DFTs, the DSMEM pushes and the
+// stores of the current tile.  The receive buffer [b][K1l][x] is reused per
+// tile: the per-tile cluster barrier (after every CTA has armed its receive
+// mbarrier and finished reading the previous tile) orders the pushes.
+// Every wait is bounded; a CTA never leaves the tile loop early, so the
+// cluster barriers stay matched.
+template <typename T, int W, int MINB>
+__global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
+    colfft4096_r16_tma_kernel(const __grid_constant__ CUtensorMap tmap, const PassDesc d) {
+  using C = typename CxT<T>::type;
+  constexpr int K = int(sizeof(C) / 8);
+  constexpr uint32_t kRecvBytes = 4096u * W / 8u * sizeof(C);
+  constexpr uint32_t kLoadBytes = 512u * W * sizeof(C);
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  C* lb = reinterpret_cast<C*>(smem_raw + ((128u - (raw & 127u)) & 127u));  // [a][q][x]
+  C* rv = lb + 512 * W;                                                       // [b][K1l][x]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(rv + 512 * W);                 // load, receive
+  // uniform across the cluster (same layout in every CTA): report, copy nothing
+  if ((smem_u32(lb) & 127u) != 0 || (reinterpret_cast<uint64_t>(&tmap) & 63u) != 0) {
+    if (threadIdx.x == 0 && d.status) atomicExch(d.status, GBFFT_ERR_INTERNAL_DEVICE);
+    return;
+  }
+  const int r = int(cg::this_cluster().block_rank());
+  const int64_t tpb = d.ncols / W;
+  const int64_t tiles = tpb * d.nbatch;
+  const int64_t cid = int64_t(blockIdx.x) >> 3, ncl = int64_t(gridDim.x) >> 3;
+  const C* __restrict__ w = static_cast<const C*>(d.tw);
+  const int64_t oes = d.out_es;
+  const uint32_t fl = d.flags;
+  const int tid = threadIdx.x;
+  const int x = tid % W;
+  const int q = tid / W;  // 0..31
+  const int b = 32 * r + q;
+  const uint32_t rv0 = smem_u32(rv), rbar = smem_u32(&bars[1]);
+
+  auto issue = [&](int64_t tile) {
+    const int64_t bo = tile / tpb;
+    const int64_t x0 = (tile - bo * tpb) * W;
+    mbar_expect_tx(&bars[0], kLoadBytes);
+    tma_load_tile(lb, &tmap, 4, int(x0 * K), 32 * r, 0, int(bo), &bars[0]);
+  };
+  if (tid == 0) {
+    prefetch_tensormap(&tmap);
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (cid < tiles) issue(cid);
+  }
+  __syncthreads();
+  bool timed_out = false;
+  int k = 0;
+  for (int64_t tile = cid; tile < tiles; tile += ncl, ++k) {
+    const uint32_t par = uint32_t(k) & 1u;
+    if (!mbar_wait_bounded(&bars[0], par, d.status)) timed_out = true;
+    // ---- phase 1: thread (x, q): DFT-16 over a of column x, b = 32r + q
+    C v[16];
+#pragma unroll
+    for (int a = 0; a < 16; ++a) {
+      C e = lb[(a * 32 + q) * W + x];
+      if (fl & F_CONJ_IN) e.y = -e.y;
+      v[a] = e;
+    }
+    __syncthreads();  // the load buffer is consumed: fetch the next tile into it
+    if (tid == 0 && tile + ncl < tiles) {
+      fence_async_smem();
+      issue(tile + ncl);
+    }
+    dft16(v);
+    apply_powers16(v, w, b);  // W^(b*K1)
+    if (tid == 0) mbar_expect_tx(&bars[1], kRecvBytes);
+    cluster_arrive_release();  // receive buffer free (previous tile read) and armed
+    cluster_wait_acquire();
+#pragma unroll
+    for (int K1 = 0; K1 < 16; ++K1) {
+      const uint32_t dst = mapa_u32(rv0 + uint32_t(((b * 2 + (K1 & 1)) * W + x) * sizeof(C)), uint32_t(K1 >> 1));
+      st_async(dst, v[K1], mapa_u32(rbar, uint32_t(K1 >> 1)));
+    }
+    if (!mbar_wait_bounded(&bars[1], par, d.status)) timed_out = true;
+    // ---- phase 2, stage 2: thread (x, K1l = q & 1, gamma = q >> 1): DFT-16 over beta
+    const int K1l = q & 1;
+    const int gamma = q >> 1;
+#pragma unroll
+    for (int beta = 0; beta < 16; ++beta) v[beta] = rv[((16 * beta + gamma) * 2 + K1l) * W + x];
+    dft16(v);
+    apply_powers16(v, w, 16 * gamma);  // W_256^(gamma*kappa)
+    __syncthreads();
+#pragma unroll
+    for (int kappa = 0; kappa < 16; ++kappa) rv[((kappa * 16 + gamma) * 2 + K1l) * W + x] = v[kappa];
+    __syncthreads();
+    // stage 3: thread (x, K1l, kappa = q >> 1): DFT-16 over gamma
+    const int kappa = q >> 1;
+#pragma unroll
+    for (int g = 0; g < 16; ++g) v[g] = rv[((kappa * 16 + g) * 2 + K1l) * W + x];
+    dft16(v);
+    const int64_t bo = tile / tpb;
+    const int64_t x0 = (tile - bo * tpb) * W;
+    C* __restrict__ out = static_cast<C*>(d.out) + bo * d.out_bs + x0;
+    const int K1 = 2 * r + K1l;
+    const T s = T(d.scale);
+#pragma unroll
+    for (int lambda = 0; lambda < 16; ++lambda) {
+      C e = v[lambda];
+      if (fl & F_SCALE) e = cscale(e, s);
+      if (fl & F_CONJ_OUT) e.y = -e.y;
+      out[int64_t(K1 + 16 * kappa + 256 * lambda) * oes + x] = e;
+    }
+  }
+  // a timed-out wait may leave a copy landing in this CTA's buffers: wait
+  // (bounded) for the load barrier's last phase before leaving
+  if (timed_out && tid == 0) mbar_wait_bounded(&bars[0], uint32_t(k > 0 ? k - 1 : 0) & 1u, nullptr);
+  // no CTA leaves while a sibling may still address its shared memory
+  cluster_arrive_release();
+  cluster_wait_acquire();
+}
+
 template <typename T, int W, int MINB>
 struct ColR16Cfg {
   static constexpr int threads = 32 * W;
@@ -522,6 +645,56 @@ struct ColCfg {
   }
 };
 
+// Tensor map of a 4096-point strided pass's input for the persistent
+// kernel: (columns in 8-byte words, b, a, batch) with row = 256a + b, box
+// W x 32 x 16 x 1.  Returns false when the layout does not fit.
+bool col_tensor_map(const PassDesc& d, int W, size_t eb, CUtensorMap* map) {
+  if (!d.use_tma || d.in_cs != 1 || (reinterpret_cast<uintptr_t>(d.in) & 15)) return false;
+  auto fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(tensor_map_encode_fn());
+  if (!fn) return false;
+  const uint64_t K = eb / 8;
+  const uint64_t es = uint64_t(d.in_es) * eb, bs = uint64_t(d.in_bs) * eb;
+  auto fits = [](uint64_t s) { return s > 0 && s % 16 == 0 && s < (uint64_t(1) << 40); };
+  if (!fits(es) || !fits(256 * es) || (d.nbatch > 1 && !fits(bs))) return false;
+  if (uint64_t(d.ncols) * K > (uint64_t(1) << 31) || d.nbatch > (int64_t(1) << 31)) return false;
+  const cuuint64_t dims[4] = {cuuint64_t(d.ncols) * K, 256, 16, cuuint64_t(d.nbatch)};
+  const cuuint64_t strides[3] = {es, 256 * es, fits(bs) ? bs : 256 * es};
+  const cuuint32_t box[4] = {cuuint32_t(W * K), 32, 16, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, const_cast<void*>(d.in), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <typename T, int W, int MINB>
+struct ColR16TmaCfg {
+  static constexpr int threads = 32 * W;
+  static inline int clusters = 0;  // co-resident clusters
+  static size_t smem() { return 128 + size_t(1024) * W * sizeof(typename CxT<T>::type) + 2 * sizeof(uint64_t); }
+  static cudaError_t prepare() {
+    auto k = colfft4096_r16_tma_kernel<T, W, MINB>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem()));
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(8 * 1024, 1, 1);
+    cfg.blockDim = dim3(threads, 1, 1);
+    cfg.dynamicSmemBytes = smem();
+    int n = 0;
+    e = cudaOccupancyMaxActiveClusters(&n, (void*)k, &cfg);
+    clusters = n > 0 ? n : 1;
+    return e;
+  }
+  static cudaError_t launch(const PassDesc& d, cudaStream_t s) {
+    const int64_t tiles = (d.ncols / W) * d.nbatch;
+    if (tiles <= 0) return cudaSuccess;
+    CUtensorMap map;
+    if (!col_tensor_map(d, W, sizeof(typename CxT<T>::type), &map)) return ColR16Cfg<T, W, W == 16 ? 2 : 3>::launch(d, s);
+    const int64_t ncl = std::min<int64_t>(tiles, clusters);
+    colfft4096_r16_tma_kernel<T, W, MINB><<<unsigned(ncl * 8), threads, smem(), s>>>(map, d);
+    return cudaGetLastError();
+  }
+};
+
 // Variants (selected by PassDesc::col_variant):
 //   0: W = 16, U = 2, 512 threads, 2 CTAs/SM
 //   1: W = 8,  U = 1, 512 threads, 3 CTAs/SM
@@ -549,6 +722,11 @@ struct ColCfg {
   X(12, float, 32, 1)         \
   X(13, float, 16, 1)
 
+// persistent tensor-fed radix-16 variants (W, min CTAs per SM)
+#define GBFFT_COLR16TMA_TABLE(X) \
+  X(14, float, 16, 1)            \
+  X(15, float, 8, 3)
+
 }  // namespace
 
 cudaError_t prepare_col_kernels() {
@@ -565,13 +743,17 @@ cudaError_t prepare_col_kernels() {
   if (e == cudaSuccess) e = ColR16Cfg<T, W, MINB>::prepare();
   GBFFT_COLR16_TABLE(X)
 #undef X
+#define X(V, T, W, MINB) \
+  if (e == cudaSuccess) e = ColR16TmaCfg<T, W, MINB>::prepare();
+  GBFFT_COLR16TMA_TABLE(X)
+#undef X
   if (e == cudaSuccess) e = ColCfg<double, 16, 2, 1>::prepare();
   return e;
 }
 
 int col_tile_width(int variant) {
   switch (variant) {
-    case 0: case 3: case 6: case 9: case 11: case 13: return 16;
+    case 0: case 3: case 6: case 9: case 11: case 13: case 14: return 16;
     case 12: return 32;
     default: return 8;
   }
@@ -590,6 +772,10 @@ cudaError_t launch_col4096(const PassDesc& d, bool dbl, cudaStream_t s) {
 #define X(V, T, W, MINB) \
   if (d.col_variant == V) return ColR16Cfg<T, W, MINB>::launch(d, s);
   GBFFT_COLR16_TABLE(X)
+#undef X
+#define X(V, T, W, MINB) \
+  if (d.col_variant == V) return ColR16TmaCfg<T, W, MINB>::launch(d, s);
+  GBFFT_COLR16TMA_TABLE(X)
 #undef X
   return cudaErrorInvalidValue;
 }

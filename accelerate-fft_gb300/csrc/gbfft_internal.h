@@ -102,6 +102,9 @@ size_t pass_smem_bytes(const PassDesc& d, bool is_double);
 int pass_grid(const PassDesc& d);
 
 // Launch one pencil pass on `stream`; returns a cudaError_t.
+// cuTensorMapEncodeTiled from the driver (nullptr when unavailable).
+void* tensor_map_encode_fn();
+
 // Name of the __global__ function launch_pass runs for d (a 16-byte aligned
 // input assumed).
 const char* pass_kernel_name(const PassDesc& d, bool is_double);

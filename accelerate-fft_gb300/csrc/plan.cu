@@ -681,7 +681,7 @@ int build_plan(gbfft_plan* p, bool dry) {
     ps.d.col_variant = 9;
     if (const char* rv = std::getenv("GBFFT_ROW_VARIANT")) ps.d.row_variant = std::atoi(rv) & 1;
     if (const char* cv = std::getenv("GBFFT_COL_VARIANT")) ps.d.col_variant = std::atoi(cv) & 15;
-    if (ps.d.col_variant > 13) ps.d.col_variant = 9;
+    if (ps.d.col_variant > 15) ps.d.col_variant = 9;
     if (ps.d.kernel == K_COL4096 && ps.d.ncols % col_tile_width(ps.d.col_variant) != 0)
       ps.d.col_variant = 8;  // 8-column tiles
     if (ps.tw_off >= 0) ps.d.tw = base + ps.tw_off;

@@ -146,16 +146,7 @@ __global__ void __launch_bounds__(W*(N / 16), (tma_minb<T, N, W, MINB, OPS>()))
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
-            cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      f = nullptr;
-    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-  }();
-  return fn;
+  return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(tensor_map_encode_fn());
 }
 
 // Rank (2..4) of the tensor map str_tensor_map builds for this pass, or 0
@@ -290,6 +281,19 @@ struct StrCfg {
   X(double, 1024, 8, 1, false, 16, 16, 4)
 
 }  // namespace
+
+void* tensor_map_encode_fn() {
+  static void* fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return f;
+  }();
+  return fn;
+}
 
 bool str_kernel_available(int n, bool dbl) {
 #define X(T, N, W, MINB, TMA, ...) \
