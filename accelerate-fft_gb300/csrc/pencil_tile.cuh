@@ -9,6 +9,18 @@ namespace gbfft {
 
 __device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
 
+// Division by a run-time divisor d (1 <= d <= 2^16) of indices x < 2^16 by a
+// multiply-high with m = ceil(2^32 / d) (division by invariant integers,
+// Granlund and Montgomery 1994): with m = 2^32/d + e, 0 <= e < 1, the error
+// x*e/2^32 < 2^-16 <= 1/d never carries floor(x/d) to the next integer.
+// Replaces the ~20-instruction integer division in the per-element index
+// arithmetic of the tile loops.
+struct FDiv {
+  uint32_t m, d;
+  __device__ __forceinline__ explicit FDiv(uint32_t dd) : m(dd > 1 ? 0xFFFFFFFFu / dd + 1u : 0u), d(dd) {}
+  __device__ __forceinline__ uint32_t div(uint32_t x) const { return d > 1 ? __umulhi(x, m) : x; }
+};
+
 template <typename C>
 __device__ __forceinline__ C ldg_c(const C* p) {
   return __ldg(p);
@@ -23,15 +35,16 @@ __device__ __forceinline__ void stage(const C* __restrict__ src, C* __restrict__
                                       const C* __restrict__ tw, int n, int Ns, int W, int pitch) {
   const int nb = n / R;
   const int total = W * nb;
+  const FDiv div_nb{uint32_t(nb)}, div_ns{uint32_t(Ns)};
   for (int f = threadIdx.x; f < total; f += blockDim.x) {
-    const int c = f / nb;
+    const int c = int(div_nb.div(uint32_t(f)));
     const int j = f - c * nb;
     const C* s = src + c * pitch;
     C* o = dst + c * pitch;
     C v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = s[spad(j + r * nb)];
-    const int p = j % Ns;
+    const int p = j - int(div_ns.div(uint32_t(j))) * Ns;
     if (Ns > 1) {
       const C* t = tw + p * (R + (R & 1));
 #pragma unroll
@@ -93,13 +106,14 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
 
   // ---- load (+ conj, chirp, zero padding) ---------------------------------
   const int total = W * n;
+  const FDiv div_w{uint32_t(W)}, div_n{uint32_t(n)};
   for (int f = threadIdx.x; f < total; f += blockDim.x) {
     int c, i;
     if (d.load_cfast) {
-      c = f % W;
-      i = f / W;
+      i = int(div_w.div(uint32_t(f)));
+      c = f - i * W;
     } else {
-      c = f / n;
+      c = int(div_n.div(uint32_t(f)));
       i = f - c * n;
     }
     const int64_t col = c0 + c;
@@ -129,10 +143,10 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
     for (int f = threadIdx.x; f < total; f += blockDim.x) {
       int c, kk;
       if (d.store_cfast) {
-        c = f % W;
-        kk = f / W;
+        kk = int(div_w.div(uint32_t(f)));
+        c = f - kk * W;
       } else {
-        c = f / n;
+        c = int(div_n.div(uint32_t(f)));
         kk = f - c * n;
       }
       const int64_t col = c0 + c;
@@ -148,7 +162,7 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
     // spectrum * filter, then the inverse DFT as conj(DFT(conj(.)))
     const C* filt = static_cast<const C*>(d.filter);
     for (int f = threadIdx.x; f < total; f += blockDim.x) {
-      const int c = f / n, kk = f - c * n;
+      const int c = int(div_n.div(uint32_t(f))), kk = f - c * n;
       C* p = res + c * d.pitch + spad(kk);
       *p = cconj(cmul(*p, filt[kk]));
     }
@@ -166,10 +180,10 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
   for (int f = threadIdx.x; f < total; f += blockDim.x) {
     int c, kk;
     if (d.store_cfast) {
-      c = f % W;
-      kk = f / W;
+      kk = int(div_w.div(uint32_t(f)));
+      c = f - kk * W;
     } else {
-      c = f / n;
+      c = int(div_n.div(uint32_t(f)));
       kk = f - c * n;
     }
     const int64_t col = c0 + c;

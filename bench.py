@@ -127,11 +127,33 @@ WORKLOADS = {
     "specconv_8x256": dict(kind="specconv", shape=(8, 256, 256, 256), dtype="c32",
                            desc="spectral convolution fwd+adjoint: 8 Gaussian random fields 256^3 "
                                 "(|k|^-5/3 spectrum) and a 256^3 complex filter, Complex Float"),
+    "ragged_2000": dict(kind="ragged", count=2000, dtype="c32",
+                        desc="ragged batch (profiling size): 2000 Complex Float transforms, lengths "
+                             "log-uniform in [16, 65536] (70% 7-smooth, 30% prime), Forward/Inverse "
+                             "p=1/2, N(0,1), one persistent launch"),
     "ragged_20000": dict(kind="ragged", count=20000, dtype="c32",
                          desc="ragged batch: 20000 Complex Float transforms, lengths log-uniform in "
                               "[16, 65536] (70% 7-smooth, 30% prime), Forward/Inverse p=1/2, N(0,1), "
                               "one persistent launch"),
 }
+
+
+# DRAM bytes (read + write) per launch of a workload's dominant kernel from one
+# ncu capture (profiles/<kernel>_<workload>.md).  Under ncu's serialised
+# replay part of a launch's writes is still in L2 when it ends, so these read
+# below the algorithmic bytes.  The ragged figure is the 2000-transform
+# capture scaled by elements (same length distribution, traffic proportional).
+NCU_TRAFFIC = {
+    "fft2d_4096": ("colfft4096_r16_kernel", 134271232 + 73015296),
+    "fft3d_256": ("strfft_tma_kernel", 134264320 + 51690752),
+    "ragged_20000": ("ragged_kernel", 1.0691e9 * 157602267 / 16295261),
+    "ragged_2000": ("ragged_kernel", 1.0691e9),
+}
+
+
+def ncu_traffic(workload, kernel):
+    t = NCU_TRAFFIC.get(workload)
+    return float(t[1]) if t and t[0] == kernel else None
 
 
 def flops_of(shape, kind):
@@ -388,7 +410,9 @@ def run_gbfft(args, wl):
                              % (nelem * elem >> 20),
                        "plan": plan.describe(), "parallelism": "replicas" if world > 1 else "single"},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                         "frac": ach / peak, "traffic": None, "peak_source": peak_kind,
+                         "frac": ach / peak,
+                         "traffic": ncu_traffic(args.workload, kernels[dom] if npass else None),
+                         "peak_source": peak_kind,
                          "kernel": "pass %d of %d (%s)" % (dom, npass, kernels[dom] if npass else "-"),
                          "bytes_alg_per_launch": bytes_pass,
                          "kernel_ms": avg_pass[dom] if npass else None},
@@ -470,7 +494,7 @@ def run_ragged(args, wl):
     value = fl * world / (ms * 1e-3) / 1e9
     peak, peak_kind = load_peaks()
     ach = bytes_alg / (ms * 1e-3) / 1e9
-    per_ms = statistics.mean(timed(True, 3, 1)) if rank == 0 else None
+    per_ms = statistics.mean(timed(True, 3, 1)) if rank == 0 and not args.no_compare else None
     # accuracy on a sample of transforms vs FP64
     rel = None
     if rank == 0 and not args.no_check:
@@ -511,7 +535,8 @@ def run_ragged(args, wl):
                        "2x%d MiB" % (total * 8 >> 20), "plan_seconds": plan_s,
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                         "frac": ach / peak, "traffic": None, "peak_source": peak_kind,
+                         "frac": ach / peak, "traffic": ncu_traffic(args.workload, "ragged_kernel"),
+                         "peak_source": peak_kind,
                          "kernel": "ragged_kernel<float> (the single persistent launch)",
                          "bytes_alg_per_launch": bytes_alg, "kernel_ms": ms},
             "per_transform_comparator": {"ms_per_step": per_ms,
@@ -701,7 +726,8 @@ def main():
     ap.add_argument("--no-cufft", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-compare", action="store_true",
-                    help="skip timing the other precision (split-FP16 vs FP32)")
+                    help="skip the comparison runs (the other precision; the ragged batch as "
+                         "one launch sequence per transform)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
