@@ -336,32 +336,36 @@ static int cap_for(bool dbl) { return dbl ? kCapC64 : kCapC32; }
 
 // Split n = n1*n2 (n1 strided first pass, n2 second) with both <= cap,
 // n1 as close to sqrt(n) as possible.
-static bool split_four_step(int64_t n, int cap, int64_t& n1, int64_t& n2, bool dbl = false) {
-  int64_t best = 0;
-  double bestd = 1e300;
+// Factorisation n = n1 * n2 of a four-step axis, both halves within one CTA.
+// Candidates are ranked by balance, with a bonus for halves that have a
+// register-resident strided kernel; `rank` picks the rank-th best (the
+// autotuner's knob), clamped to the number of candidates.
+static bool split_four_step(int64_t n, int cap, int64_t& n1, int64_t& n2, bool dbl = false, int rank = 0) {
+  std::vector<std::pair<double, int64_t>> cand;
   for (int64_t a = 2; a <= cap && a < n; ++a) {
     if (n % a) continue;
     const int64_t b = n / a;
     if (b > cap || b < 2) continue;
-    // balanced halves, and halves that have a register-resident strided kernel
     double dd = std::fabs(std::log(double(a)) - std::log(double(b)));
     if (str_kernel_available(int(a), dbl)) dd -= 2.0;
     if (str_kernel_available(int(b), dbl)) dd -= 2.0;
-    if (dd < bestd) {
-      bestd = dd;
-      best = a;
-    }
+    cand.push_back({dd, a});
   }
-  if (!best) return false;
-  n1 = best;
-  n2 = n / best;
+  if (cand.empty()) return false;
+  std::stable_sort(cand.begin(), cand.end(),
+                   [](const std::pair<double, int64_t>& x, const std::pair<double, int64_t>& y) {
+                     return x.first < y.first;
+                   });
+  const size_t k = std::min(cand.size() - 1, size_t(std::max(rank, 0)));
+  n1 = cand[k].second;
+  n2 = n / n1;
   return true;
 }
 
 // Appends the passes of one axis.  `first`: this axis reads the user's
 // input; later axes work on the output buffer.
 int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
-             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap_in) {
+             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap_in, int split_rank) {
   const bool dbl = B.dbl;
   const int cap = cap_in > 0 ? cap_in : cap_for(dbl);
   const int src = first ? R_IN : R_OUT;
@@ -405,7 +409,7 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
 
   if (is_fast_length(ax.n)) {
     int64_t n1, n2;
-    if (!split_four_step(ax.n, cap, n1, n2, dbl)) return GBFFT_ERR_UNSUPPORTED;
+    if (!split_four_step(ax.n, cap, n1, n2, dbl, split_rank)) return GBFFT_ERR_UNSUPPORTED;
     PassSpec p1 = blank_pass(), p2 = blank_pass();
     if (!B.stages_for(int(n1), p1) || !B.stages_for(int(n2), p2)) return GBFFT_ERR_UNSUPPORTED;
     B.tw4_for(ax.n, p1);
@@ -502,7 +506,7 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
   if (ax.es != 1) return GBFFT_ERR_UNSUPPORTED;
   if (ax.outer > 1 && ax.os != ax.ncols * ax.cs) return GBFFT_ERR_UNSUPPORTED;
   int64_t m1, m2;
-  if (!split_four_step(m, cap, m1, m2, dbl)) return GBFFT_ERR_UNSUPPORTED;
+  if (!split_four_step(m, cap, m1, m2, dbl, split_rank)) return GBFFT_ERR_UNSUPPORTED;
   const int64_t rows = ax.ncols * ax.outer;
   scratch1 = std::max(scratch1, rows * m);
   scratch2 = std::max(scratch2, rows * m);
@@ -599,6 +603,58 @@ using namespace gbfft;
 
 namespace gbfft {
 
+// Creates a plan.  `forced`: build with these choices (the autotuner's
+// candidates); else the autotuner cache's choice for this device and shape,
+// else -- with GBFFT_AUTOTUNE=1 -- a fresh search, else the defaults.
+int create_plan(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype, int precision,
+                const TuneChoice* forced) {
+  if (!out) return GBFFT_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (rank < 1 || rank > 3 || !dims) return GBFFT_ERR_INVALID_ARG;
+  if (kind != GBFFT_KIND_MANY && kind != GBFFT_KIND_FULL) return GBFFT_ERR_INVALID_ARG;
+  if (dtype != GBFFT_C32 && dtype != GBFFT_C64) return GBFFT_ERR_INVALID_ARG;
+  if (precision != GBFFT_PLAIN && precision != GBFFT_SPLIT_FP16) return GBFFT_ERR_INVALID_ARG;
+  int64_t total = 1;
+  for (int i = 0; i < rank; ++i) {
+    if (dims[i] < 0) return GBFFT_ERR_INVALID_ARG;
+    if (dims[i] > 0 && total > (int64_t(1) << 40) / dims[i]) return GBFFT_ERR_UNSUPPORTED;
+    total *= dims[i];
+  }
+  if (precision == GBFFT_SPLIT_FP16 && dtype != GBFFT_C32) return GBFFT_ERR_INVALID_ARG;
+  std::unique_ptr<gbfft_plan> p(new gbfft_plan);
+  p->rank = rank;
+  for (int i = 0; i < rank; ++i) p->dims[i] = dims[i];
+  p->kind = kind;
+  p->dtype = dtype;
+  p->precision = precision;
+  p->dbl = dtype == GBFFT_C64;
+  p->total = total;
+  if (cudaGetDevice(&p->device) != cudaSuccess) return GBFFT_ERR_CUDA;
+  if (prepare_kernels() != cudaSuccess) return GBFFT_ERR_CUDA;
+  if (forced) {
+    p->tune = *forced;
+  } else if (total > 0) {
+    const std::string key = tune_key(rank, dims, kind, dtype, precision);
+    TuneChoice c;
+    if (tune_lookup(key, c)) {
+      p->tune = c;
+    } else if (const char* at = std::getenv("GBFFT_AUTOTUNE"); at && at[0] == '1') {
+      if (autotune_plan(rank, dims, kind, dtype, precision, nullptr, c, nullptr) == GBFFT_OK) p->tune = c;
+    }
+  }
+  const int64_t norm = (kind == GBFFT_KIND_FULL) ? total : dims[rank - 1];
+  p->inv_norm = norm > 0 ? 1.0 / double(norm) : 1.0;
+  if (total > 0) {
+    const int st = precision == GBFFT_SPLIT_FP16 ? build_split_plan(p.get()) : build_plan(p.get(), false);
+    if (st != GBFFT_OK) {
+      gbfft_plan_destroy(p.release());
+      return st;
+    }
+  }
+  *out = p.release();
+  return GBFFT_OK;
+}
+
 int build_plan(gbfft_plan* p, bool dry) {
   Builder B;
   B.dbl = p->dbl;
@@ -634,7 +690,7 @@ int build_plan(gbfft_plan* p, bool dry) {
   for (const Axis& ax : axes) {
     if (ax.n <= 1) continue;
     const size_t before = p->passes.size();
-    int st = add_axis(B, p->passes, ax, first, s1, s2, p->desc);
+    int st = add_axis(B, p->passes, ax, first, s1, s2, p->desc, 0, p->tune.split_rank);
     if (st != GBFFT_OK) return st;
     if (p->passes.size() > before) first = false;
   }
@@ -672,13 +728,15 @@ int build_plan(gbfft_plan* p, bool dry) {
   unsigned char* base = static_cast<unsigned char*>(p->d_tables);
   p->d_status = reinterpret_cast<int*>(base + status_off);
   const bool tma = !feature_disabled("tma");
+  const gbfft::TuneChoice& tc = p->tune;
   for (PassSpec& ps : p->passes) {
     ps.d.status = p->d_status;
-    ps.d.use_tma = tma ? 1 : 0;
-    // measured defaults on GB300 (fft2D 4096^2): single-buffered rows at
-    // 4 CTAs/SM, 8-column cluster tiles at 4 CTAs/SM; env overrides for A/B
-    ps.d.row_variant = 1;
-    ps.d.col_variant = 9;
+    // tensor / bulk copies per kernel kind as chosen (defaults: measured on
+    // GB300); GBFFT_DISABLE=tma turns every one off for A/B checks
+    const int want = ps.d.kernel == K_ROW ? tc.row_tma : ps.d.kernel == K_STRIDED ? tc.str_tma : 1;
+    ps.d.use_tma = (tma && want) ? 1 : 0;
+    ps.d.row_variant = tc.row_variant;
+    ps.d.col_variant = tc.col_variant;
     if (const char* rv = std::getenv("GBFFT_ROW_VARIANT")) ps.d.row_variant = std::atoi(rv) & 1;
     if (const char* cv = std::getenv("GBFFT_COL_VARIANT")) ps.d.col_variant = std::atoi(cv) & 15;
     if (ps.d.col_variant > 15) ps.d.col_variant = 9;
@@ -689,6 +747,12 @@ int build_plan(gbfft_plan* p, bool dry) {
     if (ps.tw4hi_off >= 0) ps.d.tw4_hi = base + ps.tw4hi_off;
     if (ps.chirp_off >= 0) ps.d.chirp = base + ps.chirp_off;
     if (ps.filter_off >= 0) ps.d.filter = base + ps.filter_off;
+  }
+  if (tc.tuned) {
+    char tb[96];
+    std::snprintf(tb, sizeof tb, " tuned(row=%d%s col=%d split=%d strtma=%d)", tc.row_variant,
+                  tc.row_tma ? "t" : "", tc.col_variant, tc.split_rank, tc.str_tma);
+    p->desc += tb;
   }
   if (std::getenv("GBFFT_PLAN_DUMP")) std::fprintf(stderr, "gbfft plan: %s\n", p->desc.c_str());
   return GBFFT_OK;
@@ -792,48 +856,17 @@ int gbfft_version(void) { return 10000 * 0 + 100 * 1 + 0; }
 
 int gbfft_plan_create(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype,
                       int precision) {
-  if (!out) return GBFFT_ERR_INVALID_ARG;
-  *out = nullptr;
-  if (rank < 1 || rank > 3 || !dims) return GBFFT_ERR_INVALID_ARG;
-  if (kind != GBFFT_KIND_MANY && kind != GBFFT_KIND_FULL) return GBFFT_ERR_INVALID_ARG;
-  if (dtype != GBFFT_C32 && dtype != GBFFT_C64) return GBFFT_ERR_INVALID_ARG;
-  if (precision != GBFFT_PLAIN && precision != GBFFT_SPLIT_FP16) return GBFFT_ERR_INVALID_ARG;
-  int64_t total = 1;
-  for (int i = 0; i < rank; ++i) {
-    if (dims[i] < 0) return GBFFT_ERR_INVALID_ARG;
-    if (dims[i] > 0 && total > (int64_t(1) << 40) / dims[i]) return GBFFT_ERR_UNSUPPORTED;
-    total *= dims[i];
-  }
-  if (precision == GBFFT_SPLIT_FP16 && dtype != GBFFT_C32) return GBFFT_ERR_INVALID_ARG;
-  std::unique_ptr<gbfft_plan> p(new gbfft_plan);
-  p->rank = rank;
-  for (int i = 0; i < rank; ++i) p->dims[i] = dims[i];
-  p->kind = kind;
-  p->dtype = dtype;
-  p->precision = precision;
-  p->dbl = dtype == GBFFT_C64;
-  p->total = total;
-  if (cudaGetDevice(&p->device) != cudaSuccess) return GBFFT_ERR_CUDA;
-  if (prepare_kernels() != cudaSuccess) return GBFFT_ERR_CUDA;
-  const int64_t norm = (kind == GBFFT_KIND_FULL) ? total : dims[rank - 1];
-  p->inv_norm = norm > 0 ? 1.0 / double(norm) : 1.0;
-  if (total > 0) {
-    if (precision == GBFFT_SPLIT_FP16) {
-      int st = build_split_plan(p.get());
-      if (st != GBFFT_OK) {
-        gbfft_plan_destroy(p.release());
-        return st;
-      }
-    } else {
-      int st = build_plan(p.get(), false);
-      if (st != GBFFT_OK) {
-        gbfft_plan_destroy(p.release());
-        return st;
-      }
-    }
-  }
-  *out = p.release();
-  return GBFFT_OK;
+  return gbfft::create_plan(out, rank, dims, kind, dtype, precision, nullptr);
+}
+
+int gbfft_autotune(int rank, const int64_t* dims, int kind, int dtype, int precision, void* stream,
+                   char* report, size_t cap) {
+  if (!dims || rank < 1 || rank > 3) return GBFFT_ERR_INVALID_ARG;
+  gbfft::TuneChoice best;
+  std::string rep;
+  const int st = gbfft::autotune_plan(rank, dims, kind, dtype, precision, stream, best, &rep);
+  if (report && cap) std::snprintf(report, cap, "%s", rep.c_str());
+  return st;
 }
 
 int gbfft_plan_explain(int rank, const int64_t* dims, int kind, int dtype, int precision, char* buf,

@@ -58,6 +58,17 @@ struct Builder {
   void precompute_blue(const std::vector<std::pair<int64_t, int64_t>>& nm);
 };
 
+// Planner choices the autotuner searches over (defaults: the measured best
+// on GB300 for fft2D 4096^2).
+struct TuneChoice {
+  int row_variant = 1;  // contiguous rows: 1 single-buffered, 0 double-buffered
+  int row_tma = 1;      //   with row_variant 0: stream rows with cp.async.bulk
+  int col_variant = 9;  // 4096-point strided axes: cluster kernel variant
+  int split_rank = 0;   // four-step axes: k-th best (n1, n2) factorisation
+  int str_tma = 1;      // strided passes: tensor-copy-fed persistent kernel
+  bool tuned = false;   // set by the autotuner (or its cache)
+};
+
 cd unit_root(int64_t t, int64_t L);  // exp(-2*pi*i*t/L), exact reduction
 bool factor_device(int64_t n, std::vector<int>& out);
 bool is_fast_length(int64_t n);
@@ -87,6 +98,7 @@ struct gbfft_plan {
   size_t s2_off = 0;
   int* d_status = nullptr;  // device status word inside d_tables
   void* d_tcmat = nullptr;  // split-FP16 plans: D_hi, D_lo of the DFT-16 (4 KiB)
+  gbfft::TuneChoice tune;   // planner choices (defaults, or the autotuner's)
   std::string desc;
 };
 
@@ -96,9 +108,23 @@ struct Axis {
   int64_t n, es, cs, ncols, os, outer;  // element (o, c, i) at o*os + c*cs + i*es
 };
 int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
-             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap = 0);
+             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap = 0, int split_rank = 0);
+int build_plan(gbfft_plan* p, bool dry);
+int build_split_plan(gbfft_plan* p);
+int create_plan(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype, int precision,
+                const TuneChoice* forced);
+// Autotuner cache: key of a plan on the current device, lookup / store, and
+// the timed search itself (tune.cu).
+std::string tune_key(int rank, const int64_t* dims, int kind, int dtype, int precision);
+bool tune_lookup(const std::string& key, TuneChoice& out);
+void tune_store(const std::string& key, const TuneChoice& c, double ms);
+int autotune_plan(int rank, const int64_t* dims, int kind, int dtype, int precision, void* stream,
+                  TuneChoice& best, std::string* report);
 void* role_ptr(const gbfft_plan* p, int role, const void* in, void* out);
 int build_plan(gbfft_plan* p, bool dry);
+int build_split_plan(gbfft_plan* p);
+int create_plan(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype, int precision,
+                const TuneChoice* forced);
 int build_split_plan(gbfft_plan* p);
 int exec_passes(const gbfft_plan* p, const std::vector<PassSpec>& passes, int mode, double inv_norm,
                 const void* in, void* out, cudaStream_t s);

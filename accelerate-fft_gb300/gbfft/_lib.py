@@ -45,6 +45,10 @@ SIGNATURES = {
     "gbfft_plan_info": (_i, [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_i)]),
     "gbfft_plan_describe": (_i, [_vp, ctypes.c_char_p, _sz]),
     "gbfft_plan_pass_kernel": (_i, [_vp, _i, ctypes.c_char_p, _sz]),
+    "gbfft_autotune": (_i, [_i, _i64p, _i, _i, _i, _vp, ctypes.c_char_p, _sz]),
+    "gbfft_tune_load": (_i, [ctypes.c_char_p]),
+    "gbfft_tune_clear": (_i, []),
+    "gbfft_tune_count": (_i, []),
     "gbfft_plan_explain": (_i, [_i, _i64p, _i, _i, _i, ctypes.c_char_p, _sz]),
     "gbfft_ragged_plan_create": (_i, [ctypes.POINTER(_vp), _i64, _i64p, _i64p,
                                       ctypes.POINTER(_i), _i]),

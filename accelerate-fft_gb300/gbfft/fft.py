@@ -52,6 +52,18 @@ def _dims(shape):
     return (ctypes.c_int64 * len(shape))(*[int(s) for s in shape])
 
 
+def autotune(shape, kind="full", dtype=torch.complex64, precision="plain", stream=None):
+    """Times the candidate plans of this transform (gbfft_autotune) and caches
+    the fastest for later plan creations; returns the per-candidate report."""
+    buf = ctypes.create_string_buffer(16384)
+    shape = tuple(int(s) for s in shape)
+    L.check(L.lib().gbfft_autotune(len(shape), _dims(shape), L.KIND_FULL if kind == "full" else L.KIND_MANY,
+                                   L.C64 if dtype == torch.complex128 else L.C32,
+                                   L.SPLIT_FP16 if precision == "split_fp16" else L.PLAIN,
+                                   _stream(stream), buf, 16384), "gbfft_autotune%s" % (shape,))
+    return buf.value.decode()
+
+
 class Plan:
     """An owned plan (gbfft_plan_create / gbfft_exec / gbfft_plan_destroy)."""
 

@@ -257,6 +257,10 @@ def run_gbfft(args, wl):
     x_cpu = make_input(shape, wl["dtype"], 1234 + rank)
     x = x_cpu.to(dev)
     y = torch.empty_like(x)
+    tune_report = None
+    if not args.no_tune:
+        # plan creation with the autotuner (untimed, like any plan creation)
+        tune_report = gbfft.autotune(shape, kind=wl["kind"], dtype=dtype, precision=args.precision)
     plan = gbfft.Plan(shape, kind=wl["kind"], dtype=dtype, precision=args.precision)
     info = plan.info
     npass = info["launches"]
@@ -331,6 +335,8 @@ def run_gbfft(args, wl):
     if rank == 0 and wl["dtype"] == "c32" and not args.no_compare:
         other = "split_fp16" if args.precision == "plain" else "plain"
         try:
+            if not args.no_tune:
+                gbfft.autotune(shape, kind=wl["kind"], dtype=dtype, precision=other)
             p2 = gbfft.Plan(shape, kind=wl["kind"], dtype=dtype, precision=other)
         except Exception as exc:  # the planner rejects shapes it has no kernel for
             other_prec = {"precision": other, "unavailable": str(exc)}
@@ -408,7 +414,8 @@ def run_gbfft(args, wl):
                        "precision": args.precision, "seed": 1234,
                        "l2": "flushed (256 MiB write) between timed steps; working set 2x%d MiB"
                              % (nelem * elem >> 20),
-                       "plan": plan.describe(), "parallelism": "replicas" if world > 1 else "single"},
+                       "plan": plan.describe(), "parallelism": "replicas" if world > 1 else "single",
+                       "autotune": tune_report.strip().splitlines()[-1] if tune_report else "off"},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                          "frac": ach / peak,
                          "traffic": ncu_traffic(args.workload, kernels[dom] if npass else None),
@@ -725,6 +732,8 @@ def main():
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cufft", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="create plans with the planner defaults instead of autotuning them")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the comparison runs (the other precision; the ragged batch as "
                          "one launch sequence per transform)")

@@ -133,6 +133,26 @@ int gbfft_plan_describe(const gbfft_plan* plan, char* buf, size_t cap);
  * profiler launch lists.  No counterpart in the reference. */
 int gbfft_plan_pass_kernel(const gbfft_plan* plan, int pass, char* buf, size_t cap);
 
+/* ---- autotuner: new beyond the reference API ---------------------------
+ * The reference takes cuFFT's internal plan choice (PTX.hs:141-169).
+ * gbfft_autotune times candidate plans of this transform on the current
+ * device (row / column kernel variants, four-step factorisation, tensor-copy
+ * strided kernel) on scratch buffers it allocates and frees, on `stream`,
+ * and caches the fastest choice per (device, dims, kind, dtype, precision);
+ * every later plan creation for that key uses it.  `report` (may be NULL)
+ * receives one line per candidate.  GBFFT_AUTOTUNE=1 makes plan creation
+ * tune on a cache miss; GBFFT_TUNE_FILE=<path> loads the cache from that
+ * file on first use and appends each new result (JSON lines). */
+int gbfft_autotune(int rank, const int64_t* dims, int kind, int dtype, int precision, void* stream,
+                   char* report, size_t cap);
+/* Loads tuned choices from a JSON-lines file; returns the number of entries
+ * read (0 if the file is missing), or a negative status.  No device work. */
+int gbfft_tune_load(const char* path);
+/* Forgets every tuned choice (the file, if any, is re-read on next use). */
+int gbfft_tune_clear(void);
+/* Number of tuned choices held. */
+int gbfft_tune_count(void);
+
 /* ---- ragged batch: new beyond the reference API -------------------------
  * `count` independent 1D transforms of uneven lengths over one flat buffer,
  * executed by one persistent launch (the reference can only express this as

@@ -66,3 +66,25 @@ def test_planner_rejects_bad_arguments(gbfft_lib):
     assert explain((4, -1))[0] == 1
     assert explain((4, 4), kind=9)[0] == 1
     assert explain((4, 4), dtype=5)[0] == 1
+
+
+def test_tune_file_parser(gbfft_lib, tmp_path):
+    """The autotuner's JSON-lines cache file loads without a GPU; malformed
+    lines are skipped."""
+    from gbfft import _lib as L
+    lib = L.lib()
+    f = tmp_path / "tune.jsonl"
+    f.write_text(
+        '{"key": "devA|2|4096x4096|1|0|0", "row_variant": 1, "row_tma": 1, "col_variant": 9, '
+        '"split_rank": 0, "str_tma": 1, "ms": 0.15}\n'
+        'not json at all\n'
+        '{"key": "devA|1|65536|0|0|0", "row_variant": 0, "row_tma": 0, "col_variant": 14, '
+        '"split_rank": 2, "str_tma": 0, "ms": 0.5}\n'
+        '{"key": "devA|1|7|0|0|0", "row_variant": 1}\n')
+    lib.gbfft_tune_clear()
+    assert lib.gbfft_tune_count() == 0
+    assert lib.gbfft_tune_load(str(f).encode()) == 2
+    assert lib.gbfft_tune_count() == 2
+    assert lib.gbfft_tune_load(str(tmp_path / "missing.jsonl").encode()) == 0
+    lib.gbfft_tune_clear()
+    assert lib.gbfft_tune_count() == 0
