@@ -105,32 +105,60 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
   const C* chirp = static_cast<const C*>(d.chirp);
 
   // ---- load (+ conj, chirp, zero padding) ---------------------------------
+  // KU elements per thread per round: every global load of a round (data,
+  // then chirp) is issued before any is used, so a thread keeps several
+  // requests in flight instead of one.
+  constexpr int KU = 4;
   const int total = W * n;
+  const int step = int(blockDim.x);
   const FDiv div_w{uint32_t(W)}, div_n{uint32_t(n)};
-  for (int f = threadIdx.x; f < total; f += blockDim.x) {
-    int c, i;
-    if (d.load_cfast) {
-      i = int(div_w.div(uint32_t(f)));
-      c = f - i * W;
-    } else {
-      c = int(div_n.div(uint32_t(f)));
-      i = f - c * n;
+  for (int f0 = threadIdx.x; f0 < total; f0 += KU * step) {
+    int sidx[KU];
+    int64_t addr[KU], lidx[KU];
+    bool inr[KU], ok[KU];
+#pragma unroll
+    for (int u = 0; u < KU; ++u) {
+      const int f = f0 + u * step;
+      inr[u] = f < total;
+      int c, i;
+      if (d.load_cfast) {
+        i = int(div_w.div(uint32_t(f)));
+        c = f - i * W;
+      } else {
+        c = int(div_n.div(uint32_t(f)));
+        i = f - c * n;
+      }
+      const int64_t col = c0 + c;
+      bool valid = inr[u] && col < d.ncols;
+      int64_t l = 0;
+      if (fl & (F_PAD_IN | F_CHIRP_IN)) {
+        l = int64_t(i) * d.lin_es + col * d.lin_cs;
+        if ((fl & F_PAD_IN) && l >= d.n_in) valid = false;
+      }
+      ok[u] = valid;
+      lidx[u] = l;
+      sidx[u] = c * d.pitch + spad(i);
+      addr[u] = valid ? (d.col_in_off ? d.col_in_off[col] : col * d.in_cs) + int64_t(i) * d.in_es : 0;
     }
-    const int64_t col = c0 + c;
-    C v = cmake<C>(T(0), T(0));
-    bool valid = col < d.ncols;
-    int64_t l = 0;
-    if (fl & (F_PAD_IN | F_CHIRP_IN)) {
-      l = int64_t(i) * d.lin_es + col * d.lin_cs;
-      if ((fl & F_PAD_IN) && l >= d.n_in) valid = false;
+    C v[KU];
+#pragma unroll
+    for (int u = 0; u < KU; ++u) v[u] = ok[u] ? in[addr[u]] : cmake<C>(T(0), T(0));
+    if (fl & F_CHIRP_IN) {
+      C ch[KU];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) ch[u] = ok[u] ? chirp[lidx[u]] : cmake<C>(T(0), T(0));
+#pragma unroll
+      for (int u = 0; u < KU; ++u) {
+        if (fl & F_CONJ_IN) v[u].y = -v[u].y;
+        v[u] = cmul(v[u], ch[u]);
+      }
+    } else if (fl & F_CONJ_IN) {
+#pragma unroll
+      for (int u = 0; u < KU; ++u) v[u].y = -v[u].y;
     }
-    if (valid) {
-      const int64_t cb = d.col_in_off ? d.col_in_off[col] : col * d.in_cs;
-      v = in[cb + int64_t(i) * d.in_es];
-      if (fl & F_CONJ_IN) v.y = -v.y;
-      if (fl & F_CHIRP_IN) v = cmul(v, chirp[l]);
-    }
-    b0[c * d.pitch + spad(i)] = v;
+#pragma unroll
+    for (int u = 0; u < KU; ++u)
+      if (inr[u]) b0[sidx[u]] = v[u];
   }
   __syncthreads();
 
@@ -172,36 +200,72 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
   }
 
   // ---- store (+ twiddle, filter, chirp, scale, conj, truncation) ---------
+  // KU outputs per thread per round; the table loads of a round (four-step
+  // twiddles, filter, chirp) are issued together before the arithmetic.
   C* __restrict__ out = static_cast<C*>(d.out) + b * d.out_bs + b_hi * d.out_bs2;
   const C* tw4_lo = static_cast<const C*>(d.tw4_lo);
   const C* tw4_hi = static_cast<const C*>(d.tw4_hi);
   const C* filt = static_cast<const C*>(d.filter);
   const int64_t tw4_mask = (int64_t(1) << d.tw4_shift) - 1;
-  for (int f = threadIdx.x; f < total; f += blockDim.x) {
-    int c, kk;
-    if (d.store_cfast) {
-      kk = int(div_w.div(uint32_t(f)));
-      c = f - kk * W;
-    } else {
-      c = int(div_n.div(uint32_t(f)));
-      kk = f - c * n;
+  const T sc = (fl & F_SCALE) ? T(d.scale) : T(1);
+  for (int f0 = threadIdx.x; f0 < total; f0 += KU * step) {
+    C v[KU];
+    int64_t oaddr[KU], lidx[KU], tt[KU];
+    bool ok[KU];
+#pragma unroll
+    for (int u = 0; u < KU; ++u) {
+      const int f = f0 + u * step;
+      int c, kk;
+      if (d.store_cfast) {
+        kk = int(div_w.div(uint32_t(f)));
+        c = f - kk * W;
+      } else {
+        c = int(div_n.div(uint32_t(f)));
+        kk = f - c * n;
+      }
+      const int64_t col = c0 + c;
+      bool valid = f < total && col < d.ncols;
+      const int64_t l = int64_t(kk) * d.lout_es + col * d.lout_cs;
+      if ((fl & F_TRUNC_OUT) && l >= d.n_out) valid = false;
+      ok[u] = valid;
+      lidx[u] = valid ? l : 0;
+      // e < N/n and kk < n, so the four-step exponent stays below N
+      tt[u] = valid ? ((fl & F_TW4_BATCH) ? b : col) * int64_t(kk) : 0;
+      v[u] = valid ? res[c * d.pitch + spad(kk)] : cmake<C>(T(0), T(0));
+      oaddr[u] = valid ? (d.col_out_off ? d.col_out_off[col] : col * d.out_cs) + int64_t(kk) * d.out_es : 0;
     }
-    const int64_t col = c0 + c;
-    if (col >= d.ncols) continue;
-    int64_t l = int64_t(kk) * d.lout_es + col * d.lout_cs;
-    if ((fl & F_TRUNC_OUT) && l >= d.n_out) continue;
-    C v = res[c * d.pitch + spad(kk)];
     if (fl & F_TW4) {
-      const int64_t e = (fl & F_TW4_BATCH) ? b : col;
-      const int64_t t = e * int64_t(kk);  // e < N/n and kk < n, so t < N
-      v = cmul(v, cmul(tw4_hi[t >> d.tw4_shift], tw4_lo[t & tw4_mask]));
+      C wh[KU], wl[KU];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) {
+        wh[u] = tw4_hi[tt[u] >> d.tw4_shift];
+        wl[u] = tw4_lo[tt[u] & tw4_mask];
+      }
+#pragma unroll
+      for (int u = 0; u < KU; ++u) v[u] = cmul(v[u], cmul(wh[u], wl[u]));
     }
-    if (fl & F_FILTER_OUT) v = cconj(cmul(v, filt[l]));
-    if (fl & (F_BLUE | F_CHIRP_OUT)) v = cmul(cconj(v), chirp[l]);
-    if (fl & F_SCALE) v = cscale(v, T(d.scale));
-    if (fl & F_CONJ_OUT) v.y = -v.y;
-    const int64_t cb = d.col_out_off ? d.col_out_off[col] : col * d.out_cs;
-    out[cb + int64_t(kk) * d.out_es] = v;
+    if (fl & F_FILTER_OUT) {
+      C h[KU];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) h[u] = filt[lidx[u]];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) v[u] = cconj(cmul(v[u], h[u]));
+    }
+    if (fl & (F_BLUE | F_CHIRP_OUT)) {
+      C ch[KU];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) ch[u] = chirp[lidx[u]];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) v[u] = cmul(cconj(v[u]), ch[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < KU; ++u) {
+      if (!ok[u]) continue;
+      C e = v[u];
+      if (fl & F_SCALE) e = cscale(e, sc);
+      if (fl & F_CONJ_OUT) e.y = -e.y;
+      out[oaddr[u]] = e;
+    }
   }
 }
 
