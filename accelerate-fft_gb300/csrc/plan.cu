@@ -365,7 +365,8 @@ static bool split_four_step(int64_t n, int cap, int64_t& n1, int64_t& n2, bool d
 // Appends the passes of one axis.  `first`: this axis reads the user's
 // input; later axes work on the output buffer.
 int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
-             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap_in, int split_rank) {
+             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap_in, int split_rank,
+             int blue_pad) {
   const bool dbl = B.dbl;
   const int cap = cap_in > 0 ? cap_in : cap_for(dbl);
   const int src = first ? R_IN : R_OUT;
@@ -505,19 +506,60 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
   // multi-pass Bluestein: contiguous rows only
   if (ax.es != 1) return GBFFT_ERR_UNSUPPORTED;
   if (ax.outer > 1 && ax.os != ax.ncols * ax.cs) return GBFFT_ERR_UNSUPPORTED;
+  return add_bluestein_multipass(B, passes, ax, src,
+                                 bluestein_multipass_length(ax.n, cap, dbl, blue_pad ? 2.5 : 1.0), cap, split_rank,
+                                 scratch1, scratch2, desc);
+}
+
+// Padded length of a multi-pass Bluestein transform: the smallest 7-smooth
+// m >= 2n - 1, or the next power of two when that costs less, counting m
+// element-passes per four-step half, weighted `generic` for halves without a
+// register-resident strided kernel (2.5 for plans: the generic tile measured
+// 2.3-3.4x slower per element than the tensor-fed strided kernel on 65536 =
+// 256 x 256; 1.0, i.e. always the smooth length, inside the ragged executor,
+// whose strided tiles load directly).
+int64_t bluestein_multipass_length(int64_t n, int cap, bool dbl, double generic) {
+  const int64_t ms = bluestein_length(n);
+  int64_t mp = 1;
+  while (mp < 2 * n - 1) mp <<= 1;
+  auto cost = [&](int64_t m) -> double {
+    int64_t a = 0, b = 0;
+    if (!split_four_step(m, cap, a, b, dbl)) return 1e300;
+    const double ca = str_kernel_available(int(a), dbl) ? 1.0 : generic;
+    const double cb = str_kernel_available(int(b), dbl) ? 1.0 : generic;
+    return double(m) * (ca + cb);
+  };
+  return cost(mp) < cost(ms) ? mp : ms;
+}
+
+// Multi-pass Bluestein over rows of length n padded to m = m1 * m2 (three
+// passes).  With j = j1*m2 + j2 and k = k1 + m1*k2 the forward four-step
+// gives X[k] in S1 laid out [k2][k1] after its second half; the inverse DFT
+// (taken as a forward DFT of the conjugate) is decomposed with output index
+// j = j2 + m2*j1, whose first half is a DFT over k2 -- the axis the forward
+// transform has just produced in registers.  So the middle pass runs: DFT
+// over j2 -> k2, multiply by the filter, conjugate, DFT over k2 -> j2,
+// twiddle W_m^(k1*j2), transposed store; the last pass does the DFT over
+// k1 -> j1, conjugate, chirp and the first n outputs.
+//   P1:  src -> S1[j2][k1]  chirp + zero pad, DFT over j1, twiddle W_m^(j2*k1)
+//   P23: S1 -> S2[k1][j2]   DFT over j2, filter, conj, DFT over k2, W_m^(k1*j2)
+//   P4:  S2 -> dst          DFT over k1, conj, chirp, y[j2 + m2*j1] for j < n
+int add_bluestein_multipass(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, int src, int64_t m,
+                            int cap, int split_rank, int64_t& scratch1, int64_t& scratch2, std::string& desc) {
+  const bool dbl = B.dbl;
+  char buf[256];
   int64_t m1, m2;
   if (!split_four_step(m, cap, m1, m2, dbl, split_rank)) return GBFFT_ERR_UNSUPPORTED;
   const int64_t rows = ax.ncols * ax.outer;
   scratch1 = std::max(scratch1, rows * m);
   scratch2 = std::max(scratch2, rows * m);
-  PassSpec p[4] = {blank_pass(), blank_pass(), blank_pass(), blank_pass()};
-  for (int i = 0; i < 4; ++i) {
-    if (!B.stages_for(int((i % 2 == 0) ? m1 : m2), p[i])) return GBFFT_ERR_UNSUPPORTED;
+  PassSpec p[3] = {blank_pass(), blank_pass(), blank_pass()};
+  for (int i = 0; i < 3; ++i) {
+    if (!B.stages_for(int(i == 1 ? m2 : m1), p[i])) return GBFFT_ERR_UNSUPPORTED;
     B.blue_for(ax.n, m, p[i]);
     p[i].d.nbatch = p[i].d.nb_lo = rows;
   }
-  // P1: src -> S1, chirp + zero pad, first four-step half, transposed store
-  {
+  {  // P1: column j2 < m2 of x[j1*m2 + j2] (j < n, else zero), out S1[j2*m1 + k1]
     PassDesc& d = p[0].d;
     B.tw4_for(m, p[0]);
     d.in_bs = ax.cs;
@@ -532,38 +574,27 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     d.n_in = ax.n;
     d.flags |= F_PAD_IN | F_CHIRP_IN | F_TW4;
   }
-  // P2: S1 in place, second half, filter multiply + conj
-  {
+  {  // P23: column k1 < m1 of S1[j2*m1 + k1]; filter index k2*m1 + k1; out S2[k1*m2 + j2]
     PassDesc& d = p[1].d;
+    B.tw4_for(m, p[1]);
     d.in_bs = d.out_bs = m;
     d.ncols = m1;
-    d.in_cs = d.out_cs = 1;
-    d.in_es = d.out_es = m1;
+    d.in_cs = 1;
+    d.in_es = m1;
+    d.out_es = 1;
+    d.out_cs = m2;
     d.lout_es = m1;
     d.lout_cs = 1;
-    d.flags |= F_FILTER_OUT;
+    d.flags |= F_SPEC | F_TW4;
   }
-  // P3: S1 -> S2, first half of the inverse (as a forward transform)
-  {
+  {  // P4: column j2 < m2 of S2[k1*m2 + j2]; out y[j1*m2 + j2] for j < n
     PassDesc& d = p[2].d;
-    B.tw4_for(m, p[2]);
-    d.in_bs = d.out_bs = m;
-    d.ncols = m2;
-    d.in_cs = 1;
-    d.in_es = m2;
-    d.out_es = 1;
-    d.out_cs = m1;
-    d.flags |= F_TW4;
-  }
-  // P4: S2 -> dst, second half, conj + chirp, first n outputs
-  {
-    PassDesc& d = p[3].d;
     d.in_bs = m;
     d.out_bs = ax.cs;
-    d.ncols = m1;
+    d.ncols = m2;
     d.in_cs = d.out_cs = 1;
-    d.in_es = d.out_es = m1;
-    d.lout_es = m1;
+    d.in_es = d.out_es = m2;
+    d.lout_es = m2;
     d.lout_cs = 1;
     d.n_out = ax.n;
     d.flags |= F_CHIRP_OUT | F_TRUNC_OUT;
@@ -571,17 +602,15 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
   p[0].src = src;
   p[0].dst = R_S1;
   p[1].src = R_S1;
-  p[1].dst = R_S1;
-  p[2].src = R_S1;
-  p[2].dst = R_S2;
-  p[3].src = R_S2;
-  p[3].dst = R_OUT;
-  for (int i = 0; i < 4; ++i) {
+  p[1].dst = R_S2;
+  p[2].src = R_S2;
+  p[2].dst = R_OUT;
+  for (int i = 0; i < 3; ++i) {
     choose_tile(p[i], dbl);
     use_strided(p[i], dbl);
     passes.push_back(p[i]);
   }
-  std::snprintf(buf, sizeof buf, "[n=%lld bluestein m=%lld=%lldx%lld 4-pass]", (long long)ax.n,
+  std::snprintf(buf, sizeof buf, "[n=%lld bluestein m=%lld=%lldx%lld 3-pass]", (long long)ax.n,
                 (long long)m, (long long)m1, (long long)m2);
   desc += buf;
   return GBFFT_OK;
@@ -690,7 +719,7 @@ int build_plan(gbfft_plan* p, bool dry) {
   for (const Axis& ax : axes) {
     if (ax.n <= 1) continue;
     const size_t before = p->passes.size();
-    int st = add_axis(B, p->passes, ax, first, s1, s2, p->desc, 0, p->tune.split_rank);
+    int st = add_axis(B, p->passes, ax, first, s1, s2, p->desc, 0, p->tune.split_rank, p->tune.blue_pad);
     if (st != GBFFT_OK) return st;
     if (p->passes.size() > before) first = false;
   }
@@ -750,8 +779,8 @@ int build_plan(gbfft_plan* p, bool dry) {
   }
   if (tc.tuned) {
     char tb[96];
-    std::snprintf(tb, sizeof tb, " tuned(row=%d%s col=%d split=%d strtma=%d)", tc.row_variant,
-                  tc.row_tma ? "t" : "", tc.col_variant, tc.split_rank, tc.str_tma);
+    std::snprintf(tb, sizeof tb, " tuned(row=%d%s col=%d split=%d strtma=%d bluepad=%d)", tc.row_variant,
+                  tc.row_tma ? "t" : "", tc.col_variant, tc.split_rank, tc.str_tma, tc.blue_pad);
     p->desc += tb;
   }
   if (std::getenv("GBFFT_PLAN_DUMP")) std::fprintf(stderr, "gbfft plan: %s\n", p->desc.c_str());

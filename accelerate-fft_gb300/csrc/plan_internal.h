@@ -66,6 +66,7 @@ struct TuneChoice {
   int col_variant = 9;  // 4096-point strided axes: cluster kernel variant
   int split_rank = 0;   // four-step axes: k-th best (n1, n2) factorisation
   int str_tma = 1;      // strided passes: tensor-copy-fed persistent kernel
+  int blue_pad = 1;     // four-pass Bluestein: 1 power-of-two m when cheaper, 0 smallest smooth m
   bool tuned = false;   // set by the autotuner (or its cache)
 };
 
@@ -73,6 +74,7 @@ cd unit_root(int64_t t, int64_t L);  // exp(-2*pi*i*t/L), exact reduction
 bool factor_device(int64_t n, std::vector<int>& out);
 bool is_fast_length(int64_t n);
 int64_t bluestein_length(int64_t n);
+int64_t bluestein_multipass_length(int64_t n, int cap, bool dbl, double generic);
 void blue_tables(int64_t n, int64_t m, std::vector<cd>& chirp, std::vector<cd>& filter);
 void host_fft_fp64(std::vector<cd>& x);
 void choose_tile(PassSpec& ps, bool dbl);
@@ -108,7 +110,10 @@ struct Axis {
   int64_t n, es, cs, ncols, os, outer;  // element (o, c, i) at o*os + c*cs + i*es
 };
 int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
-             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap = 0, int split_rank = 0);
+             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap = 0, int split_rank = 0,
+             int blue_pad = 1);
+int add_bluestein_multipass(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, int src, int64_t m,
+                            int cap, int split_rank, int64_t& scratch1, int64_t& scratch2, std::string& desc);
 int build_plan(gbfft_plan* p, bool dry);
 int build_split_plan(gbfft_plan* p);
 int create_plan(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype, int precision,
@@ -121,6 +126,8 @@ void tune_store(const std::string& key, const TuneChoice& c, double ms);
 int autotune_plan(int rank, const int64_t* dims, int kind, int dtype, int precision, void* stream,
                   TuneChoice& best, std::string* report);
 void* role_ptr(const gbfft_plan* p, int role, const void* in, void* out);
+int add_bluestein_multipass(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, int src, int64_t m,
+                            int cap, int split_rank, int64_t& scratch1, int64_t& scratch2, std::string& desc);
 int build_plan(gbfft_plan* p, bool dry);
 int build_split_plan(gbfft_plan* p);
 int create_plan(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype, int precision,

@@ -198,10 +198,9 @@ int g_str_sms = 0;
 
 // Fused-operation sets the tensor-fed kernel is built for (no zero padding
 // or chirp on load).
-constexpr uint32_t kTmaOps[] = {SO_PLAIN, SO_TW4, SO_TW4B, SO_FILT, SO_COUT, SO_SPEC};
 constexpr int tma_slot(uint32_t ops) {
   return ops == SO_PLAIN ? 0 : ops == SO_TW4 ? 1 : ops == SO_TW4B ? 2 : ops == SO_FILT ? 3 : ops == SO_COUT ? 4
-       : ops == SO_SPEC ? 5 : -1;
+       : ops == SO_SPEC ? 5 : ops == SO_BMID ? 6 : -1;
 }
 
 template <typename T, int N, int W, int MINB, bool TMA, int... Rs>
@@ -210,7 +209,7 @@ struct StrCfg {
   static size_t smem() { return size_t(N) * W * sizeof(typename CxT<T>::type); }
   // tensor-fed kernel: alignment slack, two tile buffers, two mbarriers
   static size_t tma_smem() { return 128 + 2 * smem() + 2 * sizeof(uint64_t); }
-  static inline int tma_ctas[6] = {0, 0, 0, 0, 0, 0};  // resident CTAs per SM of each tensor-fed kernel
+  static inline int tma_ctas[7] = {0, 0, 0, 0, 0, 0, 0};  // resident CTAs per SM of each tensor-fed kernel
   template <uint32_t OPS>
   static cudaError_t prep1() {
     cudaError_t e = cudaFuncSetAttribute(strfft_kernel<T, N, W, MINB, OPS, Rs...>,
@@ -234,6 +233,7 @@ struct StrCfg {
     if (e == cudaSuccess) e = prep1<SO_COUT>();
     if (e == cudaSuccess) e = prep1<SO_SPEC>();
     if (e == cudaSuccess) e = prep1<SO_BLUE>();
+    if (e == cudaSuccess) e = prep1<SO_BMID>();
     return e;
   }
   template <uint32_t OPS>
@@ -264,6 +264,7 @@ struct StrCfg {
       case SO_COUT: return go<SO_COUT>(d, s);
       case SO_SPEC: return go<SO_SPEC>(d, s);
       case SO_BLUE: return go<SO_BLUE>(d, s);
+      case SO_BMID: return go<SO_BMID>(d, s);
       default: return cudaErrorInvalidValue;
     }
   }

@@ -189,6 +189,7 @@ enum StrOps : uint32_t {
   SO_COUT = F_CHIRP_OUT | F_TRUNC_OUT,           // Bluestein: last half, chirp, first n
   SO_SPEC = F_SPEC,                              // spectral product (second transform)
   SO_BLUE = F_PAD_IN | F_CHIRP_IN | F_BLUE | F_TRUNC_OUT,  // whole Bluestein in one tile
+  SO_BMID = F_SPEC | F_TW4,                      // Bluestein middle: filter, inverse first half, twiddle
 };
 constexpr uint32_t kStrOpMask = F_TW4 | F_TW4_BATCH | F_PAD_IN | F_CHIRP_IN | F_FILTER_OUT | F_CHIRP_OUT |
                                 F_TRUNC_OUT | F_SPEC | F_BLUE;
@@ -407,6 +408,7 @@ __device__ __forceinline__ bool str_tile_dispatch(const PassDesc& d, int64_t til
     case SO_COUT: str_tile<T, N, W, SO_COUT, Rs...>(d, tile, smem); return true;
     case SO_SPEC: str_tile<T, N, W, SO_SPEC, Rs...>(d, tile, smem); return true;
     case SO_BLUE: str_tile<T, N, W, SO_BLUE, Rs...>(d, tile, smem); return true;
+    case SO_BMID: str_tile<T, N, W, SO_BMID, Rs...>(d, tile, smem); return true;
     default: return false;
   }
 }
@@ -415,7 +417,7 @@ __device__ __forceinline__ bool str_tile_dispatch(const PassDesc& d, int64_t til
 __host__ __device__ inline bool str_ops_supported(uint32_t flags) {
   switch (flags & kStrOpMask) {
     case SO_PLAIN: case SO_TW4: case SO_TW4B: case SO_BP1: case SO_FILT: case SO_COUT: case SO_SPEC:
-    case SO_BLUE:
+    case SO_BLUE: case SO_BMID:
       return true;
     default:
       return false;

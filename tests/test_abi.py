@@ -53,7 +53,7 @@ def test_planner_choices(gbfft_lib):
     st, s = explain((65536,))
     assert st == 0 and "four-step" in s and "launches=2" in s and "scratch=0" in s
     st, s = explain((65521,))
-    assert st == 0 and "bluestein m=131072" in s and "4-pass" in s
+    assert st == 0 and "bluestein m=131072" in s and "3-pass" in s and "launches=3" in s
     st, s = explain((8192,), dtype=1)  # Complex Double: four-step above 4096
     assert st == 0 and "four-step" in s
     st, s = explain((256, 256, 256))
