@@ -390,8 +390,8 @@ __device__ __forceinline__ void row_stages_tc(float2 (&v)[E], float2* b, const f
   }
 }
 
-template <int N, int ROWS, int... Rs>
-__global__ void __launch_bounds__(ROWS*(N / 16), 1) rowfft_tc_kernel(const PassDesc d) {
+template <int N, int ROWS, int MINB, int... Rs>
+__global__ void __launch_bounds__(ROWS*(N / 16), MINB) rowfft_tc_kernel(const PassDesc d) {
   using C = float2;
   constexpr int E = 16;
   constexpr int TH = N / E;
@@ -486,38 +486,42 @@ __global__ void __launch_bounds__(ROWS*(N / 16), 1) rowfft_tc_kernel(const PassD
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tslot), "r"(kCols) : "memory");
 }
 
-template <int N, int ROWS, int... Rs>
+template <int N, int ROWS, int MINB, int... Rs>
 struct RowTcCfg {
   static constexpr int threads = ROWS * (N / 16);
   static size_t smem() { return size_t(threads / 128) * 16384 + 4096 + size_t(ROWS) * N * 8; }
   static int ctas_per_sm;
   static cudaError_t prepare() {
-    cudaError_t e = cudaFuncSetAttribute(rowfft_tc_kernel<N, ROWS, Rs...>,
+    cudaError_t e = cudaFuncSetAttribute(rowfft_tc_kernel<N, ROWS, MINB, Rs...>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem()));
     if (e != cudaSuccess) return e;
     int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rowfft_tc_kernel<N, ROWS, Rs...>, threads, smem());
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rowfft_tc_kernel<N, ROWS, MINB, Rs...>, threads, smem());
     ctas_per_sm = nb > 0 ? nb : 1;
     return e;
   }
   static cudaError_t launch(const PassDesc& d, cudaStream_t s, int sms) {
     const int64_t chunks = (d.ncols + ROWS - 1) / ROWS;
     const int64_t grid = std::min<int64_t>(chunks, int64_t(sms) * ctas_per_sm);
-    rowfft_tc_kernel<N, ROWS, Rs...><<<unsigned(grid), threads, smem(), s>>>(d);
+    rowfft_tc_kernel<N, ROWS, MINB, Rs...><<<unsigned(grid), threads, smem(), s>>>(d);
     return cudaGetLastError();
   }
 };
-template <int N, int ROWS, int... Rs>
-int RowTcCfg<N, ROWS, Rs...>::ctas_per_sm = 1;
+template <int N, int ROWS, int MINB, int... Rs>
+int RowTcCfg<N, ROWS, MINB, Rs...>::ctas_per_sm = 1;
 
 // lengths with radix-16 stages and whole warpgroups per CTA
-#define GBFFT_ROWTC_TABLE(X)  \
-  X(256, 8, 16, 16)           \
-  X(512, 4, 16, 16, 2)        \
-  X(1024, 2, 16, 16, 4)       \
-  X(2048, 1, 16, 16, 8)       \
-  X(4096, 1, 16, 16, 16)      \
-  X(8192, 1, 16, 16, 16, 2)
+// (N, rows per CTA, min CTAs per SM for row_variant 1 / 0, radices).  On
+// fft2D 4096^2 the row pass took 151 us at 2 CTAs/SM (128 registers), 177 us
+// at 3 (80 registers, spills) and 151 us at 1: the MMA round trip per stage,
+// not occupancy, bounds it.
+#define GBFFT_ROWTC_TABLE(X)        \
+  X(256, 8, 2, 1, 16, 16)           \
+  X(512, 4, 2, 1, 16, 16, 2)        \
+  X(1024, 2, 2, 1, 16, 16, 4)       \
+  X(2048, 1, 2, 3, 16, 16, 8)       \
+  X(4096, 1, 2, 3, 16, 16, 16)      \
+  X(8192, 1, 1, 1, 16, 16, 16, 2)
 
 template <typename T, int N, int E, int ROWS, int MINB, int... Rs>
 struct RowCfg {
@@ -607,7 +611,7 @@ cudaError_t prepare_row_kernels() {
 }
 
 bool row_tc_available(int n) {
-#define X(N, ROWS, ...) \
+#define X(N, ROWS, MA, MB, ...) \
   if (n == N) return true;
   GBFFT_ROWTC_TABLE(X)
 #undef X
@@ -616,8 +620,9 @@ bool row_tc_available(int n) {
 
 cudaError_t prepare_row_tc_kernels() {
   cudaError_t e = cudaSuccess;
-#define X(N, ROWS, ...) \
-  if (e == cudaSuccess) e = RowTcCfg<N, ROWS, __VA_ARGS__>::prepare();
+#define X(N, ROWS, MA, MB, ...)                                          \
+  if (e == cudaSuccess) e = RowTcCfg<N, ROWS, MA, __VA_ARGS__>::prepare(); \
+  if (e == cudaSuccess && MB != MA) e = RowTcCfg<N, ROWS, MB, __VA_ARGS__>::prepare();
   GBFFT_ROWTC_TABLE(X)
 #undef X
   return e;
@@ -625,8 +630,10 @@ cudaError_t prepare_row_tc_kernels() {
 
 cudaError_t launch_row_tc(const PassDesc& d, cudaStream_t s) {
   const int sms = g_sms > 0 ? g_sms : 1;
-#define X(N, ROWS, ...) \
-  if (d.n == N) return RowTcCfg<N, ROWS, __VA_ARGS__>::launch(d, s, sms);
+#define X(N, ROWS, MA, MB, ...)                                                           \
+  if (d.n == N)                                                                           \
+    return (d.row_variant & 1) ? RowTcCfg<N, ROWS, MA, __VA_ARGS__>::launch(d, s, sms)   \
+                               : RowTcCfg<N, ROWS, MB, __VA_ARGS__>::launch(d, s, sms);
   GBFFT_ROWTC_TABLE(X)
 #undef X
   return cudaErrorInvalidValue;
