@@ -162,11 +162,123 @@ template <int R, typename C> __device__ __forceinline__ void dft_odd(C* v) {
   for (int i = 0; i < R; ++i) v[i] = out[i];
 }
 
+// cos and sin of 2*pi*a/den at compile time: exact integer reduction to an
+// octant (8a = q*den + r) and Taylor series on [0, pi/4] (terms to x^25, well
+// below double rounding).  Used for the internal twiddles of the composite
+// radices.
+namespace cx {
+constexpr double kPi4 = 0.78539816339744830961566084581988;  // pi / 4
+constexpr double poly_sin(double x) {
+  double x2 = x * x, term = x, sum = x;
+  for (int k = 1; k <= 12; ++k) {
+    term *= -x2 / double((2 * k) * (2 * k + 1));
+    sum += term;
+  }
+  return sum;
+}
+constexpr double poly_cos(double x) {
+  double x2 = x * x, term = 1.0, sum = 1.0;
+  for (int k = 1; k <= 12; ++k) {
+    term *= -x2 / double((2 * k - 1) * (2 * k));
+    sum += term;
+  }
+  return sum;
+}
+// c = cos(2 pi a / den), s = sin(2 pi a / den)
+constexpr void cos_sin(long a, long den, double& c, double& s) {
+  a %= den;
+  if (a < 0) a += den;
+  const long q = (8 * a) / den, r = 8 * a - q * den;
+  const double phi = kPi4 * double(r) / double(den);          // angle past the octant start
+  const double psi = kPi4 * double(den - r) / double(den);    // pi/4 - phi
+  const double sp = poly_sin(phi), cp = poly_cos(phi), sq = poly_sin(psi), cq = poly_cos(psi);
+  switch (q) {
+    case 0: c = cp; s = sp; break;
+    case 1: c = sq; s = cq; break;
+    case 2: c = -sp; s = cp; break;
+    case 3: c = -cq; s = sq; break;
+    case 4: c = -cp; s = -sp; break;
+    case 5: c = -sq; s = -cq; break;
+    case 6: c = sp; s = -cp; break;
+    default: c = cq; s = -sq; break;
+  }
+}
+constexpr double cos2pi(long a, long den) {
+  double c = 0, s = 0;
+  cos_sin(a, den, c, s);
+  return c;
+}
+constexpr double sin2pi(long a, long den) {
+  double c = 0, s = 0;
+  cos_sin(a, den, c, s);
+  return s;
+}
+}  // namespace cx
+
+template <int R, typename C> __device__ __forceinline__ void dft(C* v);
+
+// v *= W_R^m = exp(-2 pi i m / R), exact for multiples of a quarter turn
+template <int R, int M, typename C> __device__ __forceinline__ C twiddle_const(C a) {
+  constexpr int m = M % R;
+  if constexpr (m == 0) {
+    return a;
+  } else if constexpr ((4 * m) % R == 0) {
+    constexpr int q = (4 * m) / R;  // quarter turns: W = (-i)^q
+    if constexpr (q == 1) return cmul_mi(a);
+    else if constexpr (q == 2) return cmake<C>(-a.x, -a.y);
+    else return cmake<C>(-a.y, a.x);
+  } else {
+    return cmulc(a, cx::cos2pi(m, R), -cx::sin2pi(m, R));
+  }
+}
+
+// Composite radix R = R1 * R2 (Cooley-Tukey inside the registers): inputs
+// j = R2*j1 + j2, outputs k = k1 + R1*k2; DFT_R1 over j1 for every j2,
+// twiddle W_R^(j2*k1), DFT_R2 over j2 for every k1.
+template <int R1, int R2, int J2, int K1, typename C>
+__device__ __forceinline__ void comp_tw(const C* t, C* y) {
+  if constexpr (K1 < R1) {
+    y[K1 * R2 + J2] = twiddle_const<R1 * R2, J2 * K1>(t[K1]);
+    comp_tw<R1, R2, J2, K1 + 1>(t, y);
+  }
+}
+template <int R1, int R2, int J2 = 0, typename C>
+__device__ __forceinline__ void comp_first(const C* v, C* y) {
+  if constexpr (J2 < R2) {
+    C t[R1];
+#pragma unroll
+    for (int j1 = 0; j1 < R1; ++j1) t[j1] = v[R2 * j1 + J2];
+    dft<R1>(t);
+    y[J2] = t[0];
+    comp_tw<R1, R2, J2, 1>(t, y);
+    comp_first<R1, R2, J2 + 1>(v, y);
+  }
+}
+template <int R1, int R2, typename C> __device__ __forceinline__ void dft_comp(C* v) {
+  C y[R1 * R2];
+  comp_first<R1, R2>(v, y);
+#pragma unroll
+  for (int k1 = 0; k1 < R1; ++k1) {
+    C t[R2];
+#pragma unroll
+    for (int j2 = 0; j2 < R2; ++j2) t[j2] = y[k1 * R2 + j2];
+    dft<R2>(t);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) v[k1 + R1 * k2] = t[k2];
+  }
+}
+
 template <int R, typename C> __device__ __forceinline__ void dft(C* v) {
   if constexpr (R == 2) dft2(v);
   else if constexpr (R == 4) dft4(v);
   else if constexpr (R == 8) dft8(v);
   else if constexpr (R == 16) dft16(v);
+  else if constexpr (R == 6) dft_comp<2, 3>(v);
+  else if constexpr (R == 9) dft_comp<3, 3>(v);
+  else if constexpr (R == 10) dft_comp<2, 5>(v);
+  else if constexpr (R == 12) dft_comp<4, 3>(v);
+  else if constexpr (R == 14) dft_comp<2, 7>(v);
+  else if constexpr (R == 15) dft_comp<3, 5>(v);
   else dft_odd<R>(v);
 }
 

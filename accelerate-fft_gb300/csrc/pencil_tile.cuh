@@ -74,6 +74,12 @@ __device__ C* run_stages(const PassDesc& d, C* b0, C* b1) {
       case 3: stage<3>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
       case 5: stage<5>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
       case 7: stage<7>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 6: stage<6>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 9: stage<9>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 10: stage<10>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 12: stage<12>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 14: stage<14>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
+      case 15: stage<15>(src, dst, t, d.n, si.ns, d.W, d.pitch); break;
       default: break;
     }
     __syncthreads();

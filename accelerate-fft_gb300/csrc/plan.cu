@@ -15,6 +15,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <functional>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -61,6 +62,11 @@ cd unit_root(int64_t t, int64_t L) {
   return cd(c2, -s2);  // exp(-i * angle)
 }
 
+// Radix list of the device Stockham stages for a 7-smooth n.  Powers of two:
+// radix 16 while possible, then 8 / 4 / 2 (the lists the register kernels are
+// instantiated with).  Lengths with odd factors: the fewest stages over
+// radices up to 16, including the composite radices 6, 9, 10, 12, 14 and 15
+// (one shared-memory round trip per stage), larger radices first on ties.
 bool factor_device(int64_t n, std::vector<int>& out) {
   out.clear();
   if (n < 1) return false;
@@ -71,19 +77,56 @@ bool factor_device(int64_t n, std::vector<int>& out) {
   while (m % 5 == 0) { m /= 5; ++a5; }
   while (m % 7 == 0) { m /= 7; ++a7; }
   if (m != 1) return false;
-  while (a2 >= 4) { out.push_back(16); a2 -= 4; }
-  if (a2 == 3) out.push_back(8);
-  else if (a2 == 2) out.push_back(4);
-  else if (a2 == 1) out.push_back(2);
-  for (int i = 0; i < a7; ++i) out.push_back(7);
-  for (int i = 0; i < a5; ++i) out.push_back(5);
-  for (int i = 0; i < a3; ++i) out.push_back(3);
+  if (a3 == 0 && a5 == 0 && a7 == 0) {
+    while (a2 >= 4) { out.push_back(16); a2 -= 4; }
+    if (a2 == 3) out.push_back(8);
+    else if (a2 == 2) out.push_back(4);
+    else if (a2 == 1) out.push_back(2);
+    return true;
+  }
+  struct Rad { int r, e2, e3, e5, e7; };
+  static const Rad rad[] = {{16, 4, 0, 0, 0}, {15, 0, 1, 1, 0}, {14, 1, 0, 0, 1}, {12, 2, 1, 0, 0},
+                            {10, 1, 0, 1, 0}, {9, 0, 2, 0, 0},  {8, 3, 0, 0, 0},  {7, 0, 0, 0, 1},
+                            {6, 1, 1, 0, 0},  {5, 0, 0, 1, 0},  {4, 2, 0, 0, 0},  {3, 0, 1, 0, 0},
+                            {2, 1, 0, 0, 0}};
+  // fewest stages for exponents (b2, b3, b5, b7), memoised; -1 = unreachable
+  std::map<int64_t, std::pair<int, int>> memo;  // key -> (stages, radix index)
+  std::function<int(int, int, int, int)> best = [&](int b2, int b3, int b5, int b7) -> int {
+    if (b2 == 0 && b3 == 0 && b5 == 0 && b7 == 0) return 0;
+    const int64_t key = ((int64_t(b2) * 64 + b3) * 64 + b5) * 64 + b7;
+    auto it = memo.find(key);
+    if (it != memo.end()) return it->second.first;
+    int bs = -1, bi = -1;
+    for (int i = 0; i < int(sizeof(rad) / sizeof(rad[0])); ++i) {
+      const Rad& r = rad[i];
+      if (r.e2 > b2 || r.e3 > b3 || r.e5 > b5 || r.e7 > b7) continue;
+      const int sub = best(b2 - r.e2, b3 - r.e3, b5 - r.e5, b7 - r.e7);
+      if (sub >= 0 && (bs < 0 || sub + 1 < bs)) {
+        bs = sub + 1;
+        bi = i;
+      }
+    }
+    memo[key] = {bs, bi};
+    return bs;
+  };
+  if (best(a2, a3, a5, a7) < 0) return false;
+  while (a2 || a3 || a5 || a7) {
+    const int64_t key = ((int64_t(a2) * 64 + a3) * 64 + a5) * 64 + a7;
+    const Rad& r = rad[memo[key].second];
+    out.push_back(r.r);
+    a2 -= r.e2;
+    a3 -= r.e3;
+    a5 -= r.e5;
+    a7 -= r.e7;
+  }
   return true;
 }
 
 bool is_fast_length(int64_t n) {
-  std::vector<int> f;
-  return factor_device(n, f);
+  if (n < 1) return false;
+  for (int p : {2, 3, 5, 7})
+    while (n % p == 0) n /= p;
+  return n == 1;
 }
 
 // FP64 Stockham FFT on the host (forward sign) for 7-smooth lengths; used
@@ -341,9 +384,29 @@ static int cap_for(bool dbl) { return dbl ? kCapC64 : kCapC32; }
 // register-resident strided kernel; `rank` picks the rank-th best (the
 // autotuner's knob), clamped to the number of candidates.
 static bool split_four_step(int64_t n, int cap, int64_t& n1, int64_t& n2, bool dbl = false, int rank = 0) {
+  // divisors of n (n is 7-smooth here): every product of its prime powers
+  std::vector<int64_t> divs{1};
+  {
+    int64_t m = n;
+    for (int p : {2, 3, 5, 7}) {
+      int e = 0;
+      while (m % p == 0) {
+        m /= p;
+        ++e;
+      }
+      const size_t k = divs.size();
+      int64_t pw = 1;
+      for (int i = 0; i < e; ++i) {
+        pw *= p;
+        for (size_t j = 0; j < k; ++j) divs.push_back(divs[j] * pw);
+      }
+    }
+    if (m != 1) return false;
+    std::sort(divs.begin(), divs.end());
+  }
   std::vector<std::pair<double, int64_t>> cand;
-  for (int64_t a = 2; a <= cap && a < n; ++a) {
-    if (n % a) continue;
+  for (int64_t a : divs) {
+    if (a < 2 || a > cap || a >= n) continue;
     const int64_t b = n / a;
     if (b > cap || b < 2) continue;
     double dd = std::fabs(std::log(double(a)) - std::log(double(b)));
@@ -474,8 +537,16 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     return GBFFT_OK;
   }
 
-  // Bluestein
-  const int64_t m = bluestein_length(ax.n);
+  // Bluestein.  Single pass: the power of two when it is at most 1/8 longer
+  // than the cheapest smooth length (radix-16 stages are the fastest per
+  // element; 1009 pads to 2048 rather than 2025 = 15 x 15 x 9), unless the
+  // autotuner chose the smooth length (blue_pad 0).
+  int64_t m = bluestein_length(ax.n);
+  if (blue_pad > 0 && m <= cap) {
+    int64_t mp = 1;
+    while (mp < 2 * ax.n - 1) mp <<= 1;
+    if (mp <= cap && 8 * mp <= 9 * m) m = mp;
+  }
   if (m <= cap) {
     PassSpec ps = blank_pass();
     if (!B.stages_for(int(m), ps)) return GBFFT_ERR_UNSUPPORTED;
@@ -507,29 +578,40 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
   if (ax.es != 1) return GBFFT_ERR_UNSUPPORTED;
   if (ax.outer > 1 && ax.os != ax.ncols * ax.cs) return GBFFT_ERR_UNSUPPORTED;
   return add_bluestein_multipass(B, passes, ax, src,
-                                 bluestein_multipass_length(ax.n, cap, dbl, blue_pad ? 2.5 : 1.0), cap, split_rank,
+                                 bluestein_multipass_length(ax.n, cap, dbl,
+                                                            blue_pad > 0    ? 2.5
+                                                            : blue_pad == 0 ? 1.0
+                                                                            : kRaggedGenericWeight),
+                                 cap, split_rank,
                                  scratch1, scratch2, desc);
 }
 
-// Padded length of a multi-pass Bluestein transform: the smallest 7-smooth
-// m >= 2n - 1, or the next power of two when that costs less, counting m
-// element-passes per four-step half, weighted `generic` for halves without a
-// register-resident strided kernel (2.5 for plans: the generic tile measured
-// 2.3-3.4x slower per element than the tensor-fed strided kernel on 65536 =
-// 256 x 256; 1.0, i.e. always the smooth length, inside the ragged executor,
-// whose strided tiles load directly).
+// Padded length of a multi-pass Bluestein transform: the 7-smooth m in
+// [2n - 1, next power of two] with the least m * (c(m1) + c(m2)), where
+// m = m1 * m2 is the four-step split and c(h) is 1 for a half with a
+// register-resident strided kernel and `generic` otherwise (2.5 for plans:
+// the generic tile measured 2.3-3.4x slower per element than the tensor-fed
+// strided kernel on 65536 = 256 x 256; the ragged executor passes its own
+// weight).  With generic = 1 this is the smallest smooth m.
 int64_t bluestein_multipass_length(int64_t n, int cap, bool dbl, double generic) {
-  const int64_t ms = bluestein_length(n);
-  int64_t mp = 1;
-  while (mp < 2 * n - 1) mp <<= 1;
-  auto cost = [&](int64_t m) -> double {
+  const int64_t lo = 2 * n - 1;
+  int64_t hi = 1;
+  while (hi < lo) hi <<= 1;
+  int64_t best = hi;
+  double best_cost = 1e300;
+  for (int64_t m = lo; m <= hi; ++m) {
+    if (!is_fast_length(m)) continue;
     int64_t a = 0, b = 0;
-    if (!split_four_step(m, cap, a, b, dbl)) return 1e300;
+    if (!split_four_step(m, cap, a, b, dbl)) continue;
     const double ca = str_kernel_available(int(a), dbl) ? 1.0 : generic;
     const double cb = str_kernel_available(int(b), dbl) ? 1.0 : generic;
-    return double(m) * (ca + cb);
-  };
-  return cost(mp) < cost(ms) ? mp : ms;
+    const double cost = double(m) * (ca + cb);
+    if (cost < best_cost) {
+      best_cost = cost;
+      best = m;
+    }
+  }
+  return best;
 }
 
 // Multi-pass Bluestein over rows of length n padded to m = m1 * m2 (three

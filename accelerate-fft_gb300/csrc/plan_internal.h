@@ -75,6 +75,10 @@ bool factor_device(int64_t n, std::vector<int>& out);
 bool is_fast_length(int64_t n);
 int64_t bluestein_length(int64_t n);
 int64_t bluestein_multipass_length(int64_t n, int cap, bool dbl, double generic);
+// Relative per-element cost of a generic-tile four-step half inside the
+// ragged executor (its strided tiles load directly, so the gap to the
+// register tiles is smaller than in plans); blue_pad = -1 in add_axis.
+constexpr double kRaggedGenericWeight = 2.0;
 void blue_tables(int64_t n, int64_t m, std::vector<cd>& chirp, std::vector<cd>& filter);
 void host_fft_fp64(std::vector<cd>& x);
 void choose_tile(PassSpec& ps, bool dbl);
@@ -111,7 +115,7 @@ struct Axis {
 };
 int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
              int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap = 0, int split_rank = 0,
-             int blue_pad = 1);
+             int blue_pad = 1);  // Bluestein padding: 1 plans' choice, 0 smallest smooth, -1 ragged
 int add_bluestein_multipass(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, int src, int64_t m,
                             int cap, int split_rank, int64_t& scratch1, int64_t& scratch2, std::string& desc);
 int build_plan(gbfft_plan* p, bool dry);

@@ -283,7 +283,7 @@ int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64
       if (lengths[i] <= 1 || is_fast_length(lengths[i])) continue;
       // the padded length add_axis will pick (single tile, or four-pass)
       int64_t m = bluestein_length(lengths[i]);
-      if (m > cap) m = bluestein_multipass_length(lengths[i], cap, dbl, 1.0);
+      if (m > cap) m = bluestein_multipass_length(lengths[i], cap, dbl, kRaggedGenericWeight);
       nm.push_back({lengths[i], m});
     }
     B.precompute_blue(nm);
@@ -295,7 +295,7 @@ int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64
     int64_t s1 = 0, s2 = 0;
     std::string desc;
     const Axis ax{n, 1, n, 1, n, 1};
-    const int st = add_axis(B, lc.passes, ax, true, s1, s2, desc, cap, 0, 0);
+    const int st = add_axis(B, lc.passes, ax, true, s1, s2, desc, cap, 0, -1);
     if (st != GBFFT_OK) return st;
     lc.m = s2;  // rows (1) * m for the four-pass Bluestein, else 0
     for (PassSpec& ps : lc.passes) {

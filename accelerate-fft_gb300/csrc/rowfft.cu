@@ -579,7 +579,7 @@ int RowCfg<T, N, E, ROWS, MINB, Rs...>::tma_ctas_per_sm = 1;
   X(float, 2048, 16, 2, 3, 16, 16, 8)        \
   X(float, 4096, 16, 1, 3, 16, 16, 16)       \
   X(float, 8192, 16, 1, 1, 16, 16, 16, 2)    \
-  X(float, 1000, 40, 4, 2, 8, 5, 5, 5)       \
+  X(float, 1000, 10, 4, 2, 10, 10, 10)       \
   X(double, 256, 16, 16, 2, 16, 16)          \
   X(double, 512, 16, 8, 2, 16, 16, 2)        \
   X(double, 1024, 16, 4, 2, 16, 16, 4)       \

@@ -241,7 +241,8 @@ int autotune_plan(int rank, const int64_t* dims, int kind, int dtype, int precis
         {&TuneChoice::col_variant, {9, 11, 13, 8, 10, 15, 14}, has_kernel(p0, K_COL4096)},
         {&TuneChoice::split_rank, {0, 1, 2}, has_flag(p0, F_TW4)},
         {&TuneChoice::str_tma, {1, 0}, has_kernel(p0, K_STRIDED)},
-        {&TuneChoice::blue_pad, {1, 0}, has_flag(p0, F_FILTER_OUT)},
+        {&TuneChoice::blue_pad, {1, 0}, has_flag(p0, F_FILTER_OUT) || has_flag(p0, F_BLUE) ||
+                                            has_flag(p0, F_SPEC | F_CHIRP_IN)},
     };
     for (const Knob& k : knobs) {
       if (!k.applies) continue;
