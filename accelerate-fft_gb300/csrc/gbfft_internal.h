@@ -115,6 +115,7 @@ cudaError_t launch_pass(const PassDesc& d, bool is_double, cudaStream_t stream);
 cudaError_t prepare_kernels();
 
 bool row_kernel_available(int n, bool dbl);
+bool row_blue_available(int m, bool dbl);  // one-pass Bluestein rows at padded length m
 cudaError_t prepare_row_kernels();
 cudaError_t launch_row(const PassDesc& d, bool dbl, cudaStream_t s);
 cudaError_t prepare_col_kernels();

@@ -45,6 +45,7 @@ cudaError_t prepare_kernels() {
 const char* pass_kernel_name(const PassDesc& d, bool dbl) {
   switch (d.kernel) {
     case K_ROW:
+      if (d.flags & F_BLUE) return "rowblue_kernel";
       if (d.row_variant & 1) return "rowfft1_kernel";
       return (d.use_tma && d.in_cs == d.n && d.out_cs == d.n) ? "rowfft_tma_kernel" : "rowfft_kernel";
     case K_COL4096:

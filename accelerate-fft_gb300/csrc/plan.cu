@@ -428,8 +428,14 @@ static bool split_four_step(int64_t n, int cap, int64_t& n1, int64_t& n2, bool d
 // Appends the passes of one axis.  `first`: this axis reads the user's
 // input; later axes work on the output buffer.
 int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
-             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap_in, int split_rank,
-             int blue_pad) {
+             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap_in, const TuneChoice* tc) {
+  const TuneChoice defaults;
+  if (!tc) tc = &defaults;
+  const int split_rank = tc->split_rank, blue_pad = tc->blue_pad;
+  // register row kernel unless chosen off; by rule, not for Complex Double
+  // with fewer rows than 64 (one FP64 row gives it only N/16 threads: the
+  // generic tile measured 29 vs 48 us on fft1D 1024)
+  const bool use_row = tc->row_kernel >= 0 ? tc->row_kernel != 0 : !(B.dbl && ax.ncols * ax.outer < 64);
   const bool dbl = B.dbl;
   const int cap = cap_in > 0 ? cap_in : cap_for(dbl);
   const int src = first ? R_IN : R_OUT;
@@ -447,7 +453,7 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     d.nbatch = d.nb_lo = ax.outer;
     choose_tile(ps, dbl);
     const char* kname = "pencil";
-    if (ax.es == 1 && ax.outer == 1 && row_kernel_available(int(ax.n), dbl) &&
+    if (ax.es == 1 && ax.outer == 1 && use_row && row_kernel_available(int(ax.n), dbl) &&
         !feature_disabled("row")) {
       d.kernel = K_ROW;
       kname = "row";
@@ -565,11 +571,14 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     d.n_in = ax.n;
     d.n_out = ax.n;
     choose_tile(ps, dbl);
+    const bool rowk =
+        ax.es == 1 && ax.outer == 1 && use_row && row_blue_available(int(m), dbl) && !feature_disabled("row");
+    if (rowk) d.kernel = K_ROW;  // register-resident rows
     ps.src = src;
     ps.dst = R_OUT;
     passes.push_back(ps);
-    std::snprintf(buf, sizeof buf, "[n=%lld bluestein m=%lld es=%lld W=%d]", (long long)ax.n,
-                  (long long)m, (long long)ax.es, ps.d.W);
+    std::snprintf(buf, sizeof buf, "[n=%lld bluestein m=%lld es=%lld %s W=%d]", (long long)ax.n,
+                  (long long)m, (long long)ax.es, rowk ? "row" : "pencil", ps.d.W);
     desc += buf;
     return GBFFT_OK;
   }
@@ -801,7 +810,7 @@ int build_plan(gbfft_plan* p, bool dry) {
   for (const Axis& ax : axes) {
     if (ax.n <= 1) continue;
     const size_t before = p->passes.size();
-    int st = add_axis(B, p->passes, ax, first, s1, s2, p->desc, 0, p->tune.split_rank, p->tune.blue_pad);
+    int st = add_axis(B, p->passes, ax, first, s1, s2, p->desc, 0, &p->tune);
     if (st != GBFFT_OK) return st;
     if (p->passes.size() > before) first = false;
   }
@@ -861,8 +870,8 @@ int build_plan(gbfft_plan* p, bool dry) {
   }
   if (tc.tuned) {
     char tb[96];
-    std::snprintf(tb, sizeof tb, " tuned(row=%d%s col=%d split=%d strtma=%d bluepad=%d)", tc.row_variant,
-                  tc.row_tma ? "t" : "", tc.col_variant, tc.split_rank, tc.str_tma, tc.blue_pad);
+    std::snprintf(tb, sizeof tb, " tuned(row=%d%s col=%d split=%d strtma=%d bluepad=%d rowk=%d)", tc.row_variant,
+                  tc.row_tma ? "t" : "", tc.col_variant, tc.split_rank, tc.str_tma, tc.blue_pad, tc.row_kernel);
     p->desc += tb;
   }
   if (std::getenv("GBFFT_PLAN_DUMP")) std::fprintf(stderr, "gbfft plan: %s\n", p->desc.c_str());
@@ -888,16 +897,20 @@ int build_split_plan(gbfft_plan* p) {
       dm[size_t(n * 32 + k)] = h;
       dm[size_t(1024 + n * 32 + k)] = __float2half_rn(float(v - double(__half2float(h))));
     }
+  // plain row passes only: one-pass Bluestein rows keep their FP32 kernel
+  auto tc_row = [](const PassSpec& ps) {
+    return ps.d.kernel == K_ROW && !(ps.d.flags & F_BLUE) && row_tc_available(ps.d.n);
+  };
   bool any = false;
   for (PassSpec& ps : p->passes)
-    if (ps.d.kernel == K_ROW && row_tc_available(ps.d.n)) any = true;
+    if (tc_row(ps)) any = true;
   if (!any) return GBFFT_OK;  // no radix-16 row pass: the plain kernels serve the plan
   if (fault_injected("alloc")) return GBFFT_ERR_ALLOC;
   if (cudaMalloc(&p->d_tcmat, dm.size() * sizeof(__half)) != cudaSuccess) return GBFFT_ERR_ALLOC;
   if (cudaMemcpy(p->d_tcmat, dm.data(), dm.size() * sizeof(__half), cudaMemcpyHostToDevice) != cudaSuccess)
     return GBFFT_ERR_CUDA;
   for (PassSpec& ps : p->passes)
-    if (ps.d.kernel == K_ROW && row_tc_available(ps.d.n)) {
+    if (tc_row(ps)) {
       ps.d.kernel = K_ROW_TC;
       ps.d.tcmat = p->d_tcmat;
     }

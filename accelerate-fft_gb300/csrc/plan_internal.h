@@ -66,7 +66,9 @@ struct TuneChoice {
   int col_variant = 9;  // 4096-point strided axes: cluster kernel variant
   int split_rank = 0;   // four-step axes: k-th best (n1, n2) factorisation
   int str_tma = 1;      // strided passes: tensor-copy-fed persistent kernel
-  int blue_pad = 1;     // four-pass Bluestein: 1 power-of-two m when cheaper, 0 smallest smooth m
+  int blue_pad = 1;     // Bluestein padding: 1 power of two when cheaper, 0 smallest smooth m,
+                        //   -1 the ragged executor's weighting
+  int row_kernel = -1;  // contiguous rows: 1 register row kernel, 0 generic tile, -1 by rule
   bool tuned = false;   // set by the autotuner (or its cache)
 };
 
@@ -77,7 +79,7 @@ int64_t bluestein_length(int64_t n);
 int64_t bluestein_multipass_length(int64_t n, int cap, bool dbl, double generic);
 // Relative per-element cost of a generic-tile four-step half inside the
 // ragged executor (its strided tiles load directly, so the gap to the
-// register tiles is smaller than in plans); blue_pad = -1 in add_axis.
+// register tiles is smaller than in plans); TuneChoice::blue_pad = -1.
 constexpr double kRaggedGenericWeight = 2.0;
 void blue_tables(int64_t n, int64_t m, std::vector<cd>& chirp, std::vector<cd>& filter);
 void host_fft_fp64(std::vector<cd>& x);
@@ -114,8 +116,8 @@ struct Axis {
   int64_t n, es, cs, ncols, os, outer;  // element (o, c, i) at o*os + c*cs + i*es
 };
 int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
-             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap = 0, int split_rank = 0,
-             int blue_pad = 1);  // Bluestein padding: 1 plans' choice, 0 smallest smooth, -1 ragged
+             int64_t& scratch1, int64_t& scratch2, std::string& desc, int cap = 0,
+             const TuneChoice* tc = nullptr);  // nullptr: the defaults
 int add_bluestein_multipass(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, int src, int64_t m,
                             int cap, int split_rank, int64_t& scratch1, int64_t& scratch2, std::string& desc);
 int build_plan(gbfft_plan* p, bool dry);

@@ -295,7 +295,9 @@ int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64
     int64_t s1 = 0, s2 = 0;
     std::string desc;
     const Axis ax{n, 1, n, 1, n, 1};
-    const int st = add_axis(B, lc.passes, ax, true, s1, s2, desc, cap, 0, -1);
+    TuneChoice rc;
+    rc.blue_pad = -1;  // the ragged executor's Bluestein weighting
+    const int st = add_axis(B, lc.passes, ax, true, s1, s2, desc, cap, &rc);
     if (st != GBFFT_OK) return st;
     lc.m = s2;  // rows (1) * m for the four-pass Bluestein, else 0
     for (PassSpec& ps : lc.passes) {

@@ -158,6 +158,78 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft1_kernel(const PassD
     }
 }
 
+// Bluestein over contiguous rows in one pass: the chirped row (n_in
+// elements, zero padded) is transformed at the padded length N in
+// registers, multiplied by the filter spectrum and conjugated, transformed
+// again straight from registers, and the first n_out outputs are
+// conjugated, multiplied by the chirp and stored.  (Both transforms are
+// forward DFTs: the inverse is taken as conj(DFT(conj(.))).)
+template <typename T, int N, int E, int ROWS, int MINB, int... Rs>
+__global__ void __launch_bounds__(ROWS*(N / E), MINB) rowblue_kernel(const PassDesc d) {
+  using C = typename CxT<T>::type;
+  constexpr int TH = N / E;
+  constexpr int R0 = rl_first(RL<Rs...>{});
+  constexpr int RZ = rl_last(RL<Rs...>{});
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int slot = threadIdx.x / TH;
+  const int t = threadIdx.x - slot * TH;
+  C* b = reinterpret_cast<C*>(smem_raw) + slot * row_pitch<N>();
+  const int64_t row = int64_t(blockIdx.x) * ROWS + slot;
+  const bool ok = row < d.ncols;
+  const uint32_t fl = d.flags;
+  const C* __restrict__ in = static_cast<const C*>(d.in) + row * d.in_cs;
+  C* __restrict__ out = static_cast<C*>(d.out) + row * d.out_cs;
+  const C* __restrict__ chirp = static_cast<const C*>(d.chirp);
+  const C* __restrict__ filt = static_cast<const C*>(d.filter);
+  const C* __restrict__ tw = static_cast<const C*>(d.tw);
+  const int nin = int(d.n_in), nout = int(d.n_out);
+  C v[E];
+  // all loads of the row first, then the chirp products
+#pragma unroll
+  for (int q = 0; q < E / R0; ++q)
+#pragma unroll
+    for (int r = 0; r < R0; ++r) {
+      const int i = t + TH * (q + r * (E / R0));
+      v[q * R0 + r] = (ok && i < nin) ? in[i] : cmake<C>(T(0), T(0));
+    }
+#pragma unroll
+  for (int q = 0; q < E / R0; ++q)
+#pragma unroll
+    for (int r = 0; r < R0; ++r) {
+      const int i = t + TH * (q + r * (E / R0));
+      C x = v[q * R0 + r];
+      if (fl & F_CONJ_IN) x.y = -x.y;
+      v[q * R0 + r] = i < nin ? cmul(x, chirp[i]) : x;
+    }
+  row_stages1<N, E, 1, 0>(v, b, tw, t, RL<Rs...>{});
+  // v[q*RZ + r] holds X[k], k = t + TH*(q + r*E/RZ); the second transform's
+  // first stage wants element t + TH*(q' + r'*E/R0) in v[q'*R0 + r']
+  C u[E];
+#pragma unroll
+  for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+    for (int r = 0; r < RZ; ++r) {
+      const int m = q + r * (E / RZ);
+      u[(m % (E / R0)) * R0 + m / (E / R0)] = cconj(cmul(v[q * RZ + r], filt[t + TH * m]));
+    }
+#pragma unroll
+  for (int i = 0; i < E; ++i) v[i] = u[i];
+  row_stages1<N, E, 1, 0>(v, b, tw, t, RL<Rs...>{});
+  if (!ok) return;
+  const T s = T(d.scale);
+#pragma unroll
+  for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+    for (int r = 0; r < RZ; ++r) {
+      const int k = t + TH * (q + r * (E / RZ));
+      if (k >= nout) continue;
+      C x = cmul(cconj(v[q * RZ + r]), chirp[k]);
+      if (fl & F_SCALE) x = cscale(x, s);
+      if (fl & F_CONJ_OUT) x.y = -x.y;
+      out[k] = x;
+    }
+}
+
 // ---- TMA-fed persistent variant (Complex Float) ----------------------------
 template <int N, int E, int ROWS, int MINB, int... Rs>
 __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_tma_kernel(const PassDesc d) {
@@ -586,6 +658,30 @@ int RowCfg<T, N, E, ROWS, MINB, Rs...>::tma_ctas_per_sm = 1;
   X(double, 2048, 16, 2, 1, 16, 16, 8)       \
   X(double, 4096, 16, 1, 1, 16, 16, 16)
 
+template <typename T, int N, int E, int ROWS, int MINB, int... Rs>
+struct RowBlueCfg {
+  static constexpr int threads = ROWS * (N / E);
+  static size_t smem() { return size_t(ROWS) * row_pitch<N>() * sizeof(typename CxT<T>::type); }
+  static cudaError_t prepare() {
+    return cudaFuncSetAttribute(rowblue_kernel<T, N, E, ROWS, MINB, Rs...>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem()));
+  }
+  static cudaError_t launch(const PassDesc& d, cudaStream_t s) {
+    const int64_t chunks = (d.ncols + ROWS - 1) / ROWS;
+    rowblue_kernel<T, N, E, ROWS, MINB, Rs...><<<unsigned(chunks), threads, smem(), s>>>(d);
+    return cudaGetLastError();
+  }
+};
+
+// one-pass Bluestein rows: (type, padded length N, E, rows per CTA, min CTAs
+// per SM, radices = factor_device(N))
+#define GBFFT_ROWBLUE_TABLE(X)              \
+  X(float, 256, 16, 16, 2, 16, 16)          \
+  X(float, 512, 16, 8, 2, 16, 16, 2)        \
+  X(float, 1024, 16, 4, 2, 16, 16, 4)       \
+  X(float, 2048, 16, 2, 2, 16, 16, 8)       \
+  X(float, 4096, 16, 1, 2, 16, 16, 16)
+
 int g_sms = 0;
 
 }  // namespace
@@ -606,6 +702,10 @@ cudaError_t prepare_row_kernels() {
 #define X(T, N, E, ROWS, MINB, ...) \
   if (e == cudaSuccess) e = RowCfg<T, N, E, ROWS, MINB, __VA_ARGS__>::prepare();
   GBFFT_ROW_TABLE(X)
+#undef X
+#define X(T, N, E, ROWS, MINB, ...) \
+  if (e == cudaSuccess) e = RowBlueCfg<T, N, E, ROWS, MINB, __VA_ARGS__>::prepare();
+  GBFFT_ROWBLUE_TABLE(X)
 #undef X
   return e;
 }
@@ -639,8 +739,23 @@ cudaError_t launch_row_tc(const PassDesc& d, cudaStream_t s) {
   return cudaErrorInvalidValue;
 }
 
+bool row_blue_available(int m, bool dbl) {
+#define X(T, N, E, ROWS, MINB, ...) \
+  if (m == N && dbl == (sizeof(T) == 8)) return true;
+  GBFFT_ROWBLUE_TABLE(X)
+#undef X
+  return false;
+}
+
 cudaError_t launch_row(const PassDesc& d, bool dbl, cudaStream_t s) {
   const int sms = g_sms > 0 ? g_sms : 1;
+  if (d.flags & F_BLUE) {
+#define X(T, N, E, ROWS, MINB, ...) \
+  if (d.n == N && dbl == (sizeof(T) == 8)) return RowBlueCfg<T, N, E, ROWS, MINB, __VA_ARGS__>::launch(d, s);
+    GBFFT_ROWBLUE_TABLE(X)
+#undef X
+    return cudaErrorInvalidValue;
+  }
 #define X(T, N, E, ROWS, MINB, ...) \
   if (d.n == N && dbl == (sizeof(T) == 8)) return RowCfg<T, N, E, ROWS, MINB, __VA_ARGS__>::launch(d, s, sms);
   GBFFT_ROW_TABLE(X)

@@ -5,7 +5,8 @@
 // double-buffered exchanges, with or without bulk-copy streaming), the
 // cluster column kernel variant for 4096-point strided axes, the four-step
 // factorisation rank, the tensor-copy-fed strided kernel on or off, and the
-// four-pass Bluestein padding (power of two or smallest 7-smooth).  The
+// Bluestein padding (power of two or smallest 7-smooth) and the register
+// row kernel versus the generic tile for contiguous rows.  The
 // search is coordinate descent from the defaults: each knob that applies to
 // the plan is swept with the others held at the best so far.  Every
 // candidate runs 2 untimed and 5 timed executions (CUDA events on the
@@ -19,7 +20,7 @@
 // use and each new result is appended to it as one JSON object per line:
 //   {"key": "<device>|<rank>|<dims>|<kind>|<dtype>|<precision>",
 //    "row_variant": 1, "row_tma": 1, "col_variant": 9, "split_rank": 0,
-//    "str_tma": 1, "blue_pad": 1, "ms": 0.153}
+//    "str_tma": 1, "blue_pad": 1, "row_kernel": -1, "ms": 0.153}
 // With GBFFT_AUTOTUNE=1 a plan creation whose key is not cached runs the
 // search first.
 #include <cuda_runtime.h>
@@ -86,6 +87,7 @@ bool parse_line(const char* line, std::string& key, TuneChoice& c, double& ms) {
       !read_int(line, "str_tma", c.str_tma))
     return false;
   if (!read_int(line, "blue_pad", c.blue_pad)) c.blue_pad = 1;
+  if (!read_int(line, "row_kernel", c.row_kernel)) c.row_kernel = -1;
   const char* m = std::strstr(line, "\"ms\":");
   ms = 0;
   if (m) std::sscanf(m + 5, " %lf", &ms);
@@ -161,8 +163,9 @@ void tune_store(const std::string& key, const TuneChoice& c, double ms) {
     if (std::FILE* f = std::fopen(path, "a")) {
       std::fprintf(f,
                    "{\"key\": \"%s\", \"row_variant\": %d, \"row_tma\": %d, \"col_variant\": %d, "
-                   "\"split_rank\": %d, \"str_tma\": %d, \"blue_pad\": %d, \"ms\": %.6f}\n",
-                   key.c_str(), c.row_variant, c.row_tma, c.col_variant, c.split_rank, c.str_tma, c.blue_pad, ms);
+                   "\"split_rank\": %d, \"str_tma\": %d, \"blue_pad\": %d, \"row_kernel\": %d, \"ms\": %.6f}\n",
+                   key.c_str(), c.row_variant, c.row_tma, c.col_variant, c.split_rank, c.str_tma, c.blue_pad,
+                   c.row_kernel, ms);
       std::fclose(f);
     }
   }
@@ -220,8 +223,8 @@ int autotune_plan(int rank, const int64_t* dims, int kind, int dtype, int precis
   auto line = [&](const TuneChoice& c, double ms, const gbfft_plan* p) {
     if (!report) return;
     char b[160];
-    std::snprintf(b, sizeof b, "row=%d rowtma=%d col=%d split=%d strtma=%d bluepad=%d: %.4f ms  ",
-                  c.row_variant, c.row_tma, c.col_variant, c.split_rank, c.str_tma, c.blue_pad, ms);
+    std::snprintf(b, sizeof b, "row=%d rowtma=%d col=%d split=%d strtma=%d bluepad=%d rowk=%d: %.4f ms  ",
+                  c.row_variant, c.row_tma, c.col_variant, c.split_rank, c.str_tma, c.blue_pad, c.row_kernel, ms);
     *report += b;
     *report += p->desc;
     *report += "\n";
@@ -241,8 +244,9 @@ int autotune_plan(int rank, const int64_t* dims, int kind, int dtype, int precis
         {&TuneChoice::col_variant, {9, 11, 13, 8, 10, 15, 14}, has_kernel(p0, K_COL4096)},
         {&TuneChoice::split_rank, {0, 1, 2}, has_flag(p0, F_TW4)},
         {&TuneChoice::str_tma, {1, 0}, has_kernel(p0, K_STRIDED)},
-        {&TuneChoice::blue_pad, {1, 0}, has_flag(p0, F_FILTER_OUT) || has_flag(p0, F_BLUE) ||
-                                            has_flag(p0, F_SPEC | F_CHIRP_IN)},
+        {&TuneChoice::blue_pad, {1, 0}, has_flag(p0, F_CHIRP_IN)},
+        {&TuneChoice::row_kernel, {1, 0}, has_kernel(p0, K_ROW) || has_kernel(p0, K_ROW_TC) ||
+                                              (p0->dbl && has_kernel(p0, K_PENCIL))},
     };
     for (const Knob& k : knobs) {
       if (!k.applies) continue;
@@ -279,9 +283,9 @@ int autotune_plan(int rank, const int64_t* dims, int kind, int dtype, int precis
   tune_store(tune_key(rank, dims, kind, dtype, precision), best, best_ms);
   if (report) {
     char b[96];
-    std::snprintf(b, sizeof b, "best: row=%d rowtma=%d col=%d split=%d strtma=%d bluepad=%d %.4f ms\n",
+    std::snprintf(b, sizeof b, "best: row=%d rowtma=%d col=%d split=%d strtma=%d bluepad=%d rowk=%d %.4f ms\n",
                   best.row_variant, best.row_tma, best.col_variant, best.split_rank, best.str_tma, best.blue_pad,
-                  best_ms);
+                  best.row_kernel, best_ms);
     *report += b;
   }
   return GBFFT_OK;

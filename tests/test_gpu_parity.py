@@ -308,7 +308,8 @@ def test_kernel_variants_agree(gbfft_lib, monkeypatch, disable, rowv, colv):
              ((2, 4096, 32), "full", np.complex64), ((256, 48), "full", np.complex64),
              ((1024, 64), "full", np.complex64), ((3, 256, 32), "full", np.complex64),
              ((128, 16, 64), "full", np.complex64), ((512, 16), "full", np.complex128),
-             ((64, 64, 16), "full", np.complex64)]
+             ((64, 64, 16), "full", np.complex64), ((33, 1009), "many", np.complex64),
+             ((5, 4001), "many", np.complex64), ((210, 243), "full", np.complex64)]
     for shape, kind, dt in cases:
         x = uniform_complex(rng, shape, dt)
         plan = g.Plan(shape, kind=kind, dtype=torch.complex64 if dt == np.complex64 else torch.complex128)
