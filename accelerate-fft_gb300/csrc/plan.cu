@@ -836,6 +836,7 @@ int build_plan(gbfft_plan* p, bool dry) {
     p->s2_off = b1;
     p->scratch_bytes = b1 + size_t(s2) * eb;
     if (cudaMalloc(&p->d_scratch, p->scratch_bytes) != cudaSuccess) return GBFFT_ERR_ALLOC;
+    if (cudaEventCreateWithFlags(&p->scratch_ev, cudaEventDisableTiming) != cudaSuccess) return GBFFT_ERR_CUDA;
   }
   // L2 policy: a pass whose output a later pass reads back stores it with
   // evict_last; every pass after the first streams its input (evict_first)
@@ -928,8 +929,32 @@ void* role_ptr(const gbfft_plan* p, int role, const void* in, void* out) {
   return nullptr;
 }
 
+// Orders executions of a plan with scratch that run on different streams
+// (see gbfft_plan::scratch_ev); a no-op for plans without scratch.
+class ScratchOrder {
+ public:
+  ScratchOrder(const gbfft_plan* p, cudaStream_t s) : p_(p), s_(s) {
+    if (!p->d_scratch || !p->scratch_ev) return;
+    lk_ = std::unique_lock<std::mutex>(p->scratch_mu);
+    if (p->scratch_used && p->scratch_stream != s) cudaStreamWaitEvent(s, p->scratch_ev, 0);
+  }
+  ~ScratchOrder() {
+    if (!lk_.owns_lock()) return;
+    if (cudaEventRecord(p_->scratch_ev, s_) == cudaSuccess) {
+      p_->scratch_stream = s_;
+      p_->scratch_used = true;
+    }
+  }
+
+ private:
+  const gbfft_plan* p_;
+  cudaStream_t s_;
+  std::unique_lock<std::mutex> lk_;
+};
+
 int exec_passes(const gbfft_plan* p, const std::vector<PassSpec>& passes, int mode, double inv_norm,
                 const void* in, void* out, cudaStream_t s) {
+  const ScratchOrder order(p, s);
   if (passes.empty()) {
     // every axis has length <= 1: the DFT is the identity
     const size_t bytes = size_t(p->total) * (p->dbl ? 16 : 8);
@@ -1023,6 +1048,7 @@ int gbfft_plan_destroy(gbfft_plan* plan) {
   if (plan->d_tables) cudaFree(plan->d_tables);
   if (plan->d_scratch) cudaFree(plan->d_scratch);
   if (plan->d_tcmat) cudaFree(plan->d_tcmat);
+  if (plan->scratch_ev) cudaEventDestroy(plan->scratch_ev);
   delete plan;
   return GBFFT_OK;
 }
@@ -1124,6 +1150,7 @@ int gbfft_exec_range(const gbfft_plan* plan, int mode, int first, int count, con
   if (plan->total == 0 || count == 0) return GBFFT_OK;
   if (!d_in || !d_out || d_in == d_out) return GBFFT_ERR_INVALID_ARG;
   const size_t last = plan->passes.size() - 1;
+  const ScratchOrder order(plan, static_cast<cudaStream_t>(stream));
   for (int i = first; i < first + count; ++i) {
     const PassSpec& ps = plan->passes[size_t(i)];
     PassDesc d = ps.d;

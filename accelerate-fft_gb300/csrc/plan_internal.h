@@ -5,6 +5,7 @@
 #include <complex>
 #include <cstdint>
 #include <map>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -108,6 +109,13 @@ struct gbfft_plan {
   void* d_tcmat = nullptr;  // split-FP16 plans: D_hi, D_lo of the DFT-16 (4 KiB)
   gbfft::TuneChoice tune;   // planner choices (defaults, or the autotuner's)
   std::string desc;
+  // Plans with scratch: executions on different streams share it, so each
+  // one waits for the previous one (an event recorded after it) when the
+  // stream changes.  Plans without scratch carry no execution state.
+  mutable std::mutex scratch_mu;
+  mutable cudaEvent_t scratch_ev = nullptr;
+  mutable cudaStream_t scratch_stream = nullptr;
+  mutable bool scratch_used = false;
 };
 
 

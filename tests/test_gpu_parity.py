@@ -275,6 +275,33 @@ def test_plan_cache_and_concurrent_streams(gbfft_lib):
         assert rel_l2(o.cpu().numpy(), ref) < 2e-6
 
 
+@pytest.mark.parametrize("shape,kind", [((6, 40009), "many"), ((16, 10007), "many")])
+def test_scratch_plan_on_concurrent_streams(gbfft_lib, shape, kind):
+    """A plan with scratch (multi-pass Bluestein) run on several streams at
+    once, each stream with its own input: the executions are ordered on the
+    shared scratch."""
+    g = gbfft_lib
+    rng = np.random.default_rng(8)
+    plan = g.Plan(shape, kind=kind, dtype=torch.complex64)
+    assert plan.info["workspace_bytes"] > 0
+    xs = [uniform_complex(rng, shape, np.complex64) for _ in range(4)]
+    ts = [torch.from_numpy(x).cuda() for x in xs]
+    torch.cuda.synchronize()
+    streams = [torch.cuda.Stream() for _ in range(4)]
+    outs = []
+    for rep in range(3):
+        for t, s in zip(ts, streams):
+            with torch.cuda.stream(s):
+                outs.append(plan("forward", t, stream=s))
+    torch.cuda.synchronize()
+    for i, o in enumerate(outs):
+        x = xs[i % 4]
+        ref = np.fft.fft(x.astype(np.complex128), axis=-1) if kind == "many" else \
+            np.fft.fftn(x.astype(np.complex128))
+        assert rel_l2(o.cpu().numpy(), ref) < 4e-6, (i, plan.describe())
+    plan.close()
+
+
 def test_fault_injection_alloc(gbfft_lib, monkeypatch):
     import ctypes
     from gbfft import _lib as L
