@@ -25,6 +25,7 @@
 #include "gbfft.h"
 #include "pencil_tile.cuh"
 #include "plan_internal.h"
+#include "strided_tile.cuh"
 
 namespace gbfft {
 
@@ -107,6 +108,132 @@ __global__ void __launch_bounds__(kSpecThreads) specconv_bwd_z_kernel(const Spec
   }
 }
 
+// Register-resident adjoint z stage for z lengths with a strided register
+// kernel: W adjacent columns per CTA, thread (x, t) holds elements t + TH*m of
+// its column (TH = N/16).  Per field the z DFTs of x~ and g~ run in
+// registers with their exchanges in one shared buffer; the thread's own
+// (k, x) slots of H (staged once) and of the g_H accumulator live in shared
+// memory, so the elementwise step needs no barrier; the first axis of the
+// adjoint inverse runs straight from registers and is stored in place.
+template <typename T, int N, int W, int... Rs>
+__global__ void __launch_bounds__(W*(N / 16), sizeof(T) == 4 ? 2 : 1) specconv_bwd_z_reg(const SpecBwdArgs a) {
+  using C = typename CxT<T>::type;
+  constexpr int E = 16;
+  constexpr int TH = N / E;
+  constexpr int R0 = rl_first(RL<Rs...>{});
+  constexpr int RZ = rl_last(RL<Rs...>{});
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* xb = reinterpret_cast<C*>(smem_raw);  // exchange buffer [i][x]
+  C* hs = xb + N * W;                      // H of the tile [k][x]
+  C* acc = hs + N * W;                     // g_H accumulator [k][x]
+  const int x = threadIdx.x % W;
+  const int t = threadIdx.x / W;
+  const int64_t col = int64_t(blockIdx.x) * W + x;
+  const bool ok = col < a.S;
+  const int64_t S = a.S;
+  const C* __restrict__ H = static_cast<const C*>(a.H);
+  const C* __restrict__ tw = static_cast<const C*>(a.z.tw);
+  const T invN = T(a.invN);
+  const C zero = cmake<C>(T(0), T(0));
+#pragma unroll
+  for (int m = 0; m < E; ++m) {
+    const int k = t + TH * m;
+    hs[k * W + x] = ok ? H[int64_t(k) * S + col] : zero;
+    acc[k * W + x] = zero;
+  }
+  for (int64_t b = 0; b < a.batch; ++b) {
+    const C* __restrict__ xt = static_cast<const C*>(a.xt) + b * a.N;
+    C* __restrict__ g = static_cast<C*>(a.g) + b * a.N;
+    C vx[E], vg[E];
+#pragma unroll
+    for (int q = 0; q < E / R0; ++q)
+#pragma unroll
+      for (int r = 0; r < R0; ++r) {
+        const int i = t + TH * (q + r * (E / R0));
+        vx[q * R0 + r] = ok ? xt[int64_t(i) * S + col] : zero;
+        vg[q * R0 + r] = ok ? g[int64_t(i) * S + col] : zero;
+      }
+    str_stages<N, E, 1, 0, W>(vx, xb, tw, t, x, RL<Rs...>{});
+    str_stages<N, E, 1, 0, W>(vg, xb, tw, t, x, RL<Rs...>{});
+    // outputs k = t + TH*m sit in v[q*RZ + r], m = q + r*E/RZ; the third
+    // transform's first stage wants element t + TH*m in u[(m % (E/R0))*R0 + m/(E/R0)]
+    C u[E];
+#pragma unroll
+    for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+      for (int r = 0; r < RZ; ++r) {
+        const int m = q + r * (E / RZ);
+        const int o = (t + TH * m) * W + x;
+        const C gy = cscale(vg[q * RZ + r], invN);
+        acc[o] = cadd(acc[o], cmul(cconj(vx[q * RZ + r]), gy));
+        u[(m % (E / R0)) * R0 + m / (E / R0)] = cmul(hs[o], cconj(gy));
+      }
+    str_stages<N, E, 1, 0, W>(u, xb, tw, t, x, RL<Rs...>{});
+    if (ok) {
+#pragma unroll
+      for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+        for (int r = 0; r < RZ; ++r) g[int64_t(t + TH * (q + r * (E / RZ))) * S + col] = u[q * RZ + r];
+    }
+  }
+  if (ok) {
+    C* __restrict__ gH = static_cast<C*>(a.gH);
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      const int k = t + TH * m;
+      gH[int64_t(k) * S + col] = acc[k * W + x];
+    }
+  }
+}
+
+// (type, N, W, radices = factor_device(N)) of the register adjoint kernel
+#define GBFFT_SPECBWD_TABLE(X)      \
+  X(float, 64, 16, 16, 4)           \
+  X(float, 128, 16, 16, 8)          \
+  X(float, 256, 16, 16, 16)         \
+  X(float, 512, 16, 16, 16, 2)      \
+  X(double, 256, 8, 16, 16)
+
+template <typename T, int N, int W, int... Rs>
+struct SpecBwdCfg {
+  static constexpr int threads = W * (N / 16);
+  static size_t smem() { return size_t(3) * N * W * sizeof(typename CxT<T>::type); }
+  static cudaError_t prepare() {
+    return cudaFuncSetAttribute(specconv_bwd_z_reg<T, N, W, Rs...>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(smem()));
+  }
+  static cudaError_t launch(const SpecBwdArgs& a, cudaStream_t s) {
+    const unsigned grid = unsigned((a.S + W - 1) / W);
+    specconv_bwd_z_reg<T, N, W, Rs...><<<grid, threads, smem(), s>>>(a);
+    return cudaGetLastError();
+  }
+};
+
+bool spec_bwd_reg_available(int n, bool dbl) {
+#define X(T, N, W, ...) \
+  if (n == N && dbl == (sizeof(T) == 8)) return true;
+  GBFFT_SPECBWD_TABLE(X)
+#undef X
+  return false;
+}
+
+cudaError_t spec_bwd_reg_prepare() {
+  cudaError_t e = cudaSuccess;
+#define X(T, N, W, ...) \
+  if (e == cudaSuccess) e = SpecBwdCfg<T, N, W, __VA_ARGS__>::prepare();
+  GBFFT_SPECBWD_TABLE(X)
+#undef X
+  return e;
+}
+
+cudaError_t spec_bwd_reg_launch(const SpecBwdArgs& a, bool dbl, cudaStream_t s) {
+#define X(T, N, W, ...) \
+  if (a.z.n == N && dbl == (sizeof(T) == 8)) return SpecBwdCfg<T, N, W, __VA_ARGS__>::launch(a, s);
+  GBFFT_SPECBWD_TABLE(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
 }  // namespace
 }  // namespace gbfft
 
@@ -121,6 +248,7 @@ struct gbfft_specconv_plan {
   PassSpec px, py, pz;    // x, y passes; z pass with the spectral product
   PassSpec pzb;           // z stages for the adjoint kernel (W, pitch of its tiles)
   size_t bwd_smem = 0;
+  bool bwd_reg = false;   // the register-resident adjoint z kernel serves this z length
 };
 
 namespace {
@@ -215,6 +343,8 @@ int gbfft_specconv_plan_create(gbfft_specconv_plan** out, int64_t batch, int64_t
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(p->bwd_smem)) !=
       cudaSuccess)
     return GBFFT_ERR_CUDA;
+  if (spec_bwd_reg_prepare() != cudaSuccess) return GBFFT_ERR_CUDA;
+  p->bwd_reg = spec_bwd_reg_available(int(d), dbl) && !feature_disabled("strided");
   *out = p.release();
   return GBFFT_OK;
 }
@@ -257,12 +387,16 @@ int gbfft_specconv_bwd(const gbfft_specconv_plan* p, const void* x, const void* 
   a.N = p->N;
   a.S = p->h * p->w;
   a.invN = 1.0 / double(p->N);
-  const unsigned grid = unsigned((a.S + a.z.W - 1) / a.z.W);
-  if (p->dbl)
-    specconv_bwd_z_kernel<double><<<grid, kSpecThreads, p->bwd_smem, s>>>(a);
-  else
-    specconv_bwd_z_kernel<float><<<grid, kSpecThreads, p->bwd_smem, s>>>(a);
-  if (cudaGetLastError() != cudaSuccess) return GBFFT_ERR_CUDA;
+  if (p->bwd_reg) {
+    if (spec_bwd_reg_launch(a, p->dbl, s) != cudaSuccess) return GBFFT_ERR_CUDA;
+  } else {
+    const unsigned grid = unsigned((a.S + a.z.W - 1) / a.z.W);
+    if (p->dbl)
+      specconv_bwd_z_kernel<double><<<grid, kSpecThreads, p->bwd_smem, s>>>(a);
+    else
+      specconv_bwd_z_kernel<float><<<grid, kSpecThreads, p->bwd_smem, s>>>(a);
+    if (cudaGetLastError() != cudaSuccess) return GBFFT_ERR_CUDA;
+  }
   st = run(p, p->py, gx, gx, 0, 1.0, nullptr, s);
   if (st == GBFFT_OK) st = run(p, p->px, gx, gx, F_CONJ_OUT, 1.0, nullptr, s);
   return st;
