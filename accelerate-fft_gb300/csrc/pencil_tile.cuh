@@ -111,19 +111,19 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
   const C* chirp = static_cast<const C*>(d.chirp);
 
   // ---- load (+ conj, chirp, zero padding) ---------------------------------
-  // KU elements per thread per round: every global load of a round (data,
+  // KL elements per thread per round: every global load of a round (data,
   // then chirp) is issued before any is used, so a thread keeps several
   // requests in flight instead of one.
-  constexpr int KU = 4;
+  constexpr int KL = 8;
   const int total = W * n;
   const int step = int(blockDim.x);
   const FDiv div_w{uint32_t(W)}, div_n{uint32_t(n)};
-  for (int f0 = threadIdx.x; f0 < total; f0 += KU * step) {
-    int sidx[KU];
-    int64_t addr[KU], lidx[KU];
-    bool inr[KU], ok[KU];
+  for (int f0 = threadIdx.x; f0 < total; f0 += KL * step) {
+    int sidx[KL];
+    int64_t addr[KL], lidx[KL];
+    bool inr[KL], ok[KL];
 #pragma unroll
-    for (int u = 0; u < KU; ++u) {
+    for (int u = 0; u < KL; ++u) {
       const int f = f0 + u * step;
       inr[u] = f < total;
       int c, i;
@@ -146,24 +146,24 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
       sidx[u] = c * d.pitch + spad(i);
       addr[u] = valid ? (d.col_in_off ? d.col_in_off[col] : col * d.in_cs) + int64_t(i) * d.in_es : 0;
     }
-    C v[KU];
+    C v[KL];
 #pragma unroll
-    for (int u = 0; u < KU; ++u) v[u] = ok[u] ? in[addr[u]] : cmake<C>(T(0), T(0));
+    for (int u = 0; u < KL; ++u) v[u] = ok[u] ? in[addr[u]] : cmake<C>(T(0), T(0));
     if (fl & F_CHIRP_IN) {
-      C ch[KU];
+      C ch[KL];
 #pragma unroll
-      for (int u = 0; u < KU; ++u) ch[u] = ok[u] ? chirp[lidx[u]] : cmake<C>(T(0), T(0));
+      for (int u = 0; u < KL; ++u) ch[u] = ok[u] ? chirp[lidx[u]] : cmake<C>(T(0), T(0));
 #pragma unroll
-      for (int u = 0; u < KU; ++u) {
+      for (int u = 0; u < KL; ++u) {
         if (fl & F_CONJ_IN) v[u].y = -v[u].y;
         v[u] = cmul(v[u], ch[u]);
       }
     } else if (fl & F_CONJ_IN) {
 #pragma unroll
-      for (int u = 0; u < KU; ++u) v[u].y = -v[u].y;
+      for (int u = 0; u < KL; ++u) v[u].y = -v[u].y;
     }
 #pragma unroll
-    for (int u = 0; u < KU; ++u)
+    for (int u = 0; u < KL; ++u)
       if (inr[u]) b0[sidx[u]] = v[u];
   }
   __syncthreads();
@@ -206,6 +206,7 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
   }
 
   // ---- store (+ twiddle, filter, chirp, scale, conj, truncation) ---------
+  constexpr int KU = 4;
   // KU outputs per thread per round; the table loads of a round (four-step
   // twiddles, filter, chirp) are issued together before the arithmetic.
   C* __restrict__ out = static_cast<C*>(d.out) + b * d.out_bs + b_hi * d.out_bs2;
