@@ -90,37 +90,29 @@ __device__ C* run_stages(const PassDesc& d, C* b0, C* b1) {
   return src;
 }
 
-// Transforms tile `tile` of pass `d` (tiles enumerate (batch, column block)).
-// `smem_raw` holds two buffers of d.W * d.pitch elements.  When
-// d.col_in_off / d.col_out_off are set, column c of the tile starts at those
-// element offsets instead of c * cs.
-template <typename T>
-__device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem_raw) {
+// Load phase of a generic tile: element i of tile column c goes to
+// b0[c*pitch + spad(i)], with conjugation, Bluestein chirp and zero padding.
+// KL elements per thread per round: every global load of a round (data, then
+// chirp) is issued before any is used.  I is the type of the per-element
+// offsets inside the tile (int when they fit in 31 bits: one widening
+// multiply-add per address instead of 64-bit products).
+template <typename T, typename I, int KL>
+__device__ __forceinline__ void pencil_load(const PassDesc& d, const typename CxT<T>::type* __restrict__ in,
+                                            typename CxT<T>::type* b0, int64_t c0, const FDiv& div_w,
+                                            const FDiv& div_n) {
   using C = typename CxT<T>::type;
-  C* b0 = reinterpret_cast<C*>(smem_raw);
-  C* b1 = b0 + d.W * d.pitch;
-
-  const int64_t tiles = (d.ncols + d.W - 1) / d.W;
-  const int64_t bq = tile / tiles;
-  const int64_t c0 = (tile - bq * tiles) * d.W;
-  const int64_t b_hi = bq / d.nb_lo;
-  const int64_t b = bq - b_hi * d.nb_lo;
   const int W = d.W, n = d.n;
-  const C* __restrict__ in = static_cast<const C*>(d.in) + b * d.in_bs + b_hi * d.in_bs2;
-  const uint32_t fl = d.flags;
-  const C* chirp = static_cast<const C*>(d.chirp);
-
-  // ---- load (+ conj, chirp, zero padding) ---------------------------------
-  // KL elements per thread per round: every global load of a round (data,
-  // then chirp) is issued before any is used, so a thread keeps several
-  // requests in flight instead of one.
-  constexpr int KL = 8;
   const int total = W * n;
   const int step = int(blockDim.x);
-  const FDiv div_w{uint32_t(W)}, div_n{uint32_t(n)};
+  const uint32_t fl = d.flags;
+  const C* __restrict__ chirp = static_cast<const C*>(d.chirp);
+  const I ies = I(d.in_es), ics = I(d.in_cs);
+  // the tile's first column (per-column offsets are absolute)
+  const C* __restrict__ base = in + (d.col_in_off ? 0 : c0 * d.in_cs);
   for (int f0 = threadIdx.x; f0 < total; f0 += KL * step) {
     int sidx[KL];
-    int64_t addr[KL], lidx[KL];
+    int64_t lidx[KL], cofs[KL];
+    I ofs[KL];
     bool inr[KL], ok[KL];
 #pragma unroll
     for (int u = 0; u < KL; ++u) {
@@ -144,11 +136,12 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
       ok[u] = valid;
       lidx[u] = l;
       sidx[u] = c * d.pitch + spad(i);
-      addr[u] = valid ? (d.col_in_off ? d.col_in_off[col] : col * d.in_cs) + int64_t(i) * d.in_es : 0;
+      ofs[u] = I(i) * ies + (d.col_in_off ? I(0) : I(c) * ics);
+      cofs[u] = (d.col_in_off && valid) ? d.col_in_off[col] : 0;
     }
     C v[KL];
 #pragma unroll
-    for (int u = 0; u < KL; ++u) v[u] = ok[u] ? in[addr[u]] : cmake<C>(T(0), T(0));
+    for (int u = 0; u < KL; ++u) v[u] = ok[u] ? base[cofs[u] + ofs[u]] : cmake<C>(T(0), T(0));
     if (fl & F_CHIRP_IN) {
       C ch[KL];
 #pragma unroll
@@ -166,6 +159,138 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
     for (int u = 0; u < KL; ++u)
       if (inr[u]) b0[sidx[u]] = v[u];
   }
+}
+
+// Store phase: output k of tile column c from res[c*pitch + spad(k)], with
+// four-step twiddle, filter, chirp, truncation, scale and conjugation.  KU
+// outputs per thread per round; the table loads of a round are issued
+// together before the arithmetic, and index work a flag does not need is
+// skipped.
+template <typename T, typename I>
+__device__ __forceinline__ void pencil_store(const PassDesc& d, typename CxT<T>::type* __restrict__ out,
+                                             const typename CxT<T>::type* res, int64_t c0, int64_t b,
+                                             const FDiv& div_w, const FDiv& div_n) {
+  using C = typename CxT<T>::type;
+  constexpr int KU = 4;
+  const int W = d.W, n = d.n;
+  const int total = W * n;
+  const int step = int(blockDim.x);
+  const uint32_t fl = d.flags;
+  const C* __restrict__ tw4_lo = static_cast<const C*>(d.tw4_lo);
+  const C* __restrict__ tw4_hi = static_cast<const C*>(d.tw4_hi);
+  const C* __restrict__ filt = static_cast<const C*>(d.filter);
+  const C* __restrict__ chirp = static_cast<const C*>(d.chirp);
+  const int64_t tw4_mask = (int64_t(1) << d.tw4_shift) - 1;
+  const T sc = (fl & F_SCALE) ? T(d.scale) : T(1);
+  const bool need_l = (fl & (F_FILTER_OUT | F_CHIRP_OUT | F_BLUE | F_TRUNC_OUT)) != 0;
+  const I oes = I(d.out_es), ocs = I(d.out_cs);
+  C* __restrict__ base = out + (d.col_out_off ? 0 : c0 * d.out_cs);
+  for (int f0 = threadIdx.x; f0 < total; f0 += KU * step) {
+    C v[KU];
+    int64_t lidx[KU], tt[KU], cofs[KU];
+    I ofs[KU];
+    bool ok[KU];
+#pragma unroll
+    for (int u = 0; u < KU; ++u) {
+      const int f = f0 + u * step;
+      int c, kk;
+      if (d.store_cfast) {
+        kk = int(div_w.div(uint32_t(f)));
+        c = f - kk * W;
+      } else {
+        c = int(div_n.div(uint32_t(f)));
+        kk = f - c * n;
+      }
+      const int64_t col = c0 + c;
+      bool valid = f < total && col < d.ncols;
+      int64_t l = 0;
+      if (need_l) {
+        l = int64_t(kk) * d.lout_es + col * d.lout_cs;
+        if ((fl & F_TRUNC_OUT) && l >= d.n_out) valid = false;
+      }
+      ok[u] = valid;
+      lidx[u] = valid ? l : 0;
+      // e < N/n and kk < n, so the four-step exponent stays below N
+      tt[u] = (valid && (fl & F_TW4)) ? ((fl & F_TW4_BATCH) ? b : col) * int64_t(kk) : 0;
+      v[u] = valid ? res[c * d.pitch + spad(kk)] : cmake<C>(T(0), T(0));
+      ofs[u] = I(kk) * oes + (d.col_out_off ? I(0) : I(c) * ocs);
+      cofs[u] = (d.col_out_off && valid) ? d.col_out_off[col] : 0;
+    }
+    if (fl & F_TW4) {
+      C wh[KU], wl[KU];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) {
+        wh[u] = tw4_hi[tt[u] >> d.tw4_shift];
+        wl[u] = tw4_lo[tt[u] & tw4_mask];
+      }
+#pragma unroll
+      for (int u = 0; u < KU; ++u) v[u] = cmul(v[u], cmul(wh[u], wl[u]));
+    }
+    if (fl & F_FILTER_OUT) {
+      C h[KU];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) h[u] = filt[lidx[u]];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) v[u] = cconj(cmul(v[u], h[u]));
+    }
+    if (fl & (F_BLUE | F_CHIRP_OUT)) {
+      C ch[KU];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) ch[u] = chirp[lidx[u]];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) v[u] = cmul(cconj(v[u]), ch[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < KU; ++u) {
+      if (!ok[u]) continue;
+      C e = v[u];
+      if (fl & F_SCALE) e = cscale(e, sc);
+      if (fl & F_CONJ_OUT) e.y = -e.y;
+      base[cofs[u] + ofs[u]] = e;
+    }
+  }
+}
+
+// True when every per-element offset inside a tile of `d` fits in 31 bits.
+__device__ __forceinline__ bool tile_idx32(const PassDesc& d) {
+  const int64_t lim = int64_t(1) << 31;
+  const int64_t in_span = int64_t(d.n - 1) * d.in_es + (d.col_in_off ? 0 : int64_t(d.W - 1) * d.in_cs);
+  const int64_t out_span = int64_t(d.n - 1) * d.out_es + (d.col_out_off ? 0 : int64_t(d.W - 1) * d.out_cs);
+  return in_span < lim && out_span < lim && d.in_es < lim && d.out_es < lim && d.in_cs < lim && d.out_cs < lim;
+}
+
+// Transforms tile `tile` of pass `d` (tiles enumerate (batch, column block)).
+// `smem_raw` holds two buffers of d.W * d.pitch elements.  When
+// d.col_in_off / d.col_out_off are set, column c of the tile starts at those
+// element offsets instead of c * cs.
+// SMALL: the caller guarantees 31-bit offsets inside every tile (the ragged
+// executor: strides within one transform), so only that version is built.
+template <typename T, bool SMALL = false>
+__device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem_raw) {
+  using C = typename CxT<T>::type;
+  C* b0 = reinterpret_cast<C*>(smem_raw);
+  C* b1 = b0 + d.W * d.pitch;
+
+  const int64_t tiles = (d.ncols + d.W - 1) / d.W;
+  const int64_t bq = tile / tiles;
+  const int64_t c0 = (tile - bq * tiles) * d.W;
+  const int64_t b_hi = bq / d.nb_lo;
+  const int64_t b = bq - b_hi * d.nb_lo;
+  const int W = d.W, n = d.n;
+  const C* __restrict__ in = static_cast<const C*>(d.in) + b * d.in_bs + b_hi * d.in_bs2;
+  const uint32_t fl = d.flags;
+
+  // ---- load (+ conj, chirp, zero padding) ---------------------------------
+  const int total = W * n;
+  const FDiv div_w{uint32_t(W)}, div_n{uint32_t(n)};
+  const bool idx32 = SMALL || tile_idx32(d);
+  // the ragged executor's tiles keep eight loads in flight per thread, the
+  // per-pass kernel four (its registers bound the resident CTAs)
+  constexpr int KL = SMALL ? 8 : 4;
+  if (idx32)
+    pencil_load<T, int, KL>(d, in, b0, c0, div_w, div_n);
+  else if constexpr (!SMALL)
+    pencil_load<T, int64_t, KL>(d, in, b0, c0, div_w, div_n);
   __syncthreads();
 
   C* res = run_stages<C>(d, b0, b1);
@@ -206,74 +331,11 @@ __device__ void pencil_tile(const PassDesc& d, int64_t tile, unsigned char* smem
   }
 
   // ---- store (+ twiddle, filter, chirp, scale, conj, truncation) ---------
-  constexpr int KU = 4;
-  // KU outputs per thread per round; the table loads of a round (four-step
-  // twiddles, filter, chirp) are issued together before the arithmetic.
   C* __restrict__ out = static_cast<C*>(d.out) + b * d.out_bs + b_hi * d.out_bs2;
-  const C* tw4_lo = static_cast<const C*>(d.tw4_lo);
-  const C* tw4_hi = static_cast<const C*>(d.tw4_hi);
-  const C* filt = static_cast<const C*>(d.filter);
-  const int64_t tw4_mask = (int64_t(1) << d.tw4_shift) - 1;
-  const T sc = (fl & F_SCALE) ? T(d.scale) : T(1);
-  for (int f0 = threadIdx.x; f0 < total; f0 += KU * step) {
-    C v[KU];
-    int64_t oaddr[KU], lidx[KU], tt[KU];
-    bool ok[KU];
-#pragma unroll
-    for (int u = 0; u < KU; ++u) {
-      const int f = f0 + u * step;
-      int c, kk;
-      if (d.store_cfast) {
-        kk = int(div_w.div(uint32_t(f)));
-        c = f - kk * W;
-      } else {
-        c = int(div_n.div(uint32_t(f)));
-        kk = f - c * n;
-      }
-      const int64_t col = c0 + c;
-      bool valid = f < total && col < d.ncols;
-      const int64_t l = int64_t(kk) * d.lout_es + col * d.lout_cs;
-      if ((fl & F_TRUNC_OUT) && l >= d.n_out) valid = false;
-      ok[u] = valid;
-      lidx[u] = valid ? l : 0;
-      // e < N/n and kk < n, so the four-step exponent stays below N
-      tt[u] = valid ? ((fl & F_TW4_BATCH) ? b : col) * int64_t(kk) : 0;
-      v[u] = valid ? res[c * d.pitch + spad(kk)] : cmake<C>(T(0), T(0));
-      oaddr[u] = valid ? (d.col_out_off ? d.col_out_off[col] : col * d.out_cs) + int64_t(kk) * d.out_es : 0;
-    }
-    if (fl & F_TW4) {
-      C wh[KU], wl[KU];
-#pragma unroll
-      for (int u = 0; u < KU; ++u) {
-        wh[u] = tw4_hi[tt[u] >> d.tw4_shift];
-        wl[u] = tw4_lo[tt[u] & tw4_mask];
-      }
-#pragma unroll
-      for (int u = 0; u < KU; ++u) v[u] = cmul(v[u], cmul(wh[u], wl[u]));
-    }
-    if (fl & F_FILTER_OUT) {
-      C h[KU];
-#pragma unroll
-      for (int u = 0; u < KU; ++u) h[u] = filt[lidx[u]];
-#pragma unroll
-      for (int u = 0; u < KU; ++u) v[u] = cconj(cmul(v[u], h[u]));
-    }
-    if (fl & (F_BLUE | F_CHIRP_OUT)) {
-      C ch[KU];
-#pragma unroll
-      for (int u = 0; u < KU; ++u) ch[u] = chirp[lidx[u]];
-#pragma unroll
-      for (int u = 0; u < KU; ++u) v[u] = cmul(cconj(v[u]), ch[u]);
-    }
-#pragma unroll
-    for (int u = 0; u < KU; ++u) {
-      if (!ok[u]) continue;
-      C e = v[u];
-      if (fl & F_SCALE) e = cscale(e, sc);
-      if (fl & F_CONJ_OUT) e.y = -e.y;
-      out[oaddr[u]] = e;
-    }
-  }
+  if (idx32)
+    pencil_store<T, int>(d, out, res, c0, b, div_w, div_n);
+  else if constexpr (!SMALL)
+    pencil_store<T, int64_t>(d, out, res, c0, b, div_w, div_n);
 }
 
 

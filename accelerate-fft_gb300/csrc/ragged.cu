@@ -80,7 +80,7 @@ __device__ __noinline__ void ragged_str(const PassDesc& d, int64_t tile, unsigne
 }
 template <typename T>
 __device__ __noinline__ void ragged_pencil(const PassDesc& d, int64_t tile, unsigned char* smem) {
-  pencil_tile<T>(d, tile, smem);
+  pencil_tile<T, true>(d, tile, smem);  // offsets within one transform fit in 31 bits
 }
 
 template <typename T>
