@@ -122,8 +122,9 @@ WORKLOADS = {
                             desc="fft innermost, Complex Float 2048x65536 (four-step), N(0,1)"),
     "many_1024x65521": dict(kind="many", shape=(1024, 65521), dtype="c32", mode="forward",
                             desc="fft innermost, Complex Float 1024x65521 (four-pass Bluestein), N(0,1)"),
-    "fft1d_1024_c64": dict(kind="full", shape=(1024,), dtype="c64", mode="forward",
-                           desc="fft1D Forward, Complex Double N=1024, U[-1,1]"),
+    "fft1d_1024_c64": dict(kind="full", shape=(1024,), dtype="c64", mode="roundtrip", dist="uniform",
+                           desc="fft1D Forward then Inverse round trip, Complex Double N=1024, "
+                                "re/im U[-1,1]"),
     "specconv_8x256": dict(kind="specconv", shape=(8, 256, 256, 256), dtype="c32",
                            desc="spectral convolution fwd+adjoint: 8 Gaussian random fields 256^3 "
                                 "(|k|^-5/3 spectrum) and a 256^3 complex filter, Complex Float"),
@@ -165,19 +166,31 @@ def flops_of(shape, kind):
     return 5.0 * rows * n * math.log2(n) if n > 1 else 0.0
 
 
-def make_input(shape, dtype, seed):
+def make_input(shape, dtype, seed, dist="normal"):
     import torch
     g = torch.Generator().manual_seed(seed)
     real_t = torch.float64 if dtype == "c64" else torch.float32
-    re = torch.randn(shape, generator=g, dtype=real_t)
-    im = torch.randn(shape, generator=g, dtype=real_t)
+    if dist == "uniform":  # i.i.d. uniform on [-1, 1]
+        re = torch.rand(shape, generator=g, dtype=real_t) * 2 - 1
+        im = torch.rand(shape, generator=g, dtype=real_t) * 2 - 1
+    else:
+        re = torch.randn(shape, generator=g, dtype=real_t)
+        im = torch.randn(shape, generator=g, dtype=real_t)
     return torch.complex(re, im)
+
+
+def step_modes(wl):
+    """Modes one step runs: a round trip is Forward then Inverse."""
+    return ("forward", "inverse") if wl["mode"] == "roundtrip" else (wl["mode"],)
 
 
 def cpu_oracle_run(wl, x_np, threads):
     from oracle import lib as O
     fn = {"full": {1: O.fft1D, 2: O.fft2D, 3: O.fft3D}[len(wl["shape"])], "many": O.fft}[wl["kind"]]
-    return fn(0 if wl["mode"] == "forward" else 2, x_np, threads=threads)
+    y = x_np
+    for m in step_modes(wl):
+        y = fn(0 if m == "forward" else 2, y, threads=threads)
+    return y
 
 
 def cpu_baseline(wl, x_np, budget_s=12.0):
@@ -199,7 +212,7 @@ def cpu_baseline(wl, x_np, budget_s=12.0):
         cpu_oracle_run(wl, sample, threads)
     dt = (time.perf_counter() - t0) / reps
     sub_shape = (rows_used,) + tuple(shape[1:]) if wl["kind"] == "many" else shape
-    fl = flops_of(sub_shape, wl["kind"])
+    fl = flops_of(sub_shape, wl["kind"]) * len(step_modes(wl))
     return {"value": fl / dt / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port",
             "sample": "%d run(s) of %s on shape %s (oracle C++ restatement of Adhoc.hs, OpenMP)"
                       % (reps, wl["desc"], "x".join(map(str, sub_shape))),
@@ -211,7 +224,7 @@ def run_reference(args, wl):
     if rank != 0:
         return
     import numpy as np
-    x = make_input(wl["shape"], wl["dtype"], 1234).numpy()
+    x = make_input(wl["shape"], wl["dtype"], 1234, wl.get("dist", "normal")).numpy()
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_oracle_run(wl, x, threads)
@@ -219,7 +232,7 @@ def run_reference(args, wl):
     for _ in range(args.steps):
         cpu_oracle_run(wl, x, threads)
     dt = (time.perf_counter() - t0) / args.steps
-    fl = flops_of(wl["shape"], wl["kind"])
+    fl = flops_of(wl["shape"], wl["kind"]) * len(step_modes(wl))
     val = fl / dt / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": "GFLOP/s", "n_gpus": world,
@@ -254,9 +267,10 @@ def run_gbfft(args, wl):
     dtype = torch.complex128 if wl["dtype"] == "c64" else torch.complex64
     elem = 16 if wl["dtype"] == "c64" else 8
     nelem = math.prod(shape)
-    x_cpu = make_input(shape, wl["dtype"], 1234 + rank)
+    x_cpu = make_input(shape, wl["dtype"], 1234 + rank, wl.get("dist", "normal"))
     x = x_cpu.to(dev)
     y = torch.empty_like(x)
+    z = torch.empty_like(x)  # round trip: the Inverse of y
     tune_report = None
     if not args.no_tune:
         # plan creation with the autotuner (untimed, like any plan creation)
@@ -265,21 +279,30 @@ def run_gbfft(args, wl):
     info = plan.info
     npass = info["launches"]
     kernels = plan.pass_kernels()
-    mode = gbfft.mode_code(wl["mode"])
+    modes = [gbfft.mode_code(m) for m in step_modes(wl)]
+    # (mode, input, output) of each transform of a step
+    ops = [(modes[0], x, y)] + ([(modes[1], y, z)] if len(modes) > 1 else [])
+    result = ops[-1][2]
+    nlaunch = npass * len(ops)
+    kernels = kernels * len(ops)
     stream = torch.cuda.current_stream(dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def one_step(events=None):
         if events is None:
-            L.check(lib.gbfft_exec(plan.handle, mode, ctypes.c_void_p(x.data_ptr()),
-                                   ctypes.c_void_p(y.data_ptr()), sp))
+            for m, a, b in ops:
+                L.check(lib.gbfft_exec(plan.handle, m, ctypes.c_void_p(a.data_ptr()),
+                                       ctypes.c_void_p(b.data_ptr()), sp))
             return
         events[0].record(stream)
-        for i in range(npass):
-            L.check(lib.gbfft_exec_range(plan.handle, mode, i, 1, ctypes.c_void_p(x.data_ptr()),
-                                         ctypes.c_void_p(y.data_ptr()), sp))
-            events[i + 1].record(stream)
+        j = 0
+        for m, a, b in ops:
+            for i in range(npass):
+                L.check(lib.gbfft_exec_range(plan.handle, m, i, 1, ctypes.c_void_p(a.data_ptr()),
+                                             ctypes.c_void_p(b.data_ptr()), sp))
+                j += 1
+                events[j].record(stream)
 
     for _ in range(args.warmup):
         one_step()
@@ -290,7 +313,7 @@ def run_gbfft(args, wl):
     if sampler:
         sampler.start()
         time.sleep(1.0)  # let nvidia-smi finish starting before the timed region
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(npass + 1)] for _ in range(args.steps)]
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(nlaunch + 1)] for _ in range(args.steps)]
     torch.cuda.synchronize()
     for k in range(args.steps):
         flush.fill_(float(k))
@@ -300,25 +323,26 @@ def run_gbfft(args, wl):
         torch.distributed.barrier()
     clocks = sampler.stop() if sampler else None
     step_ms = [e[0].elapsed_time(e[-1]) for e in evs]
-    pass_ms = [[e[i].elapsed_time(e[i + 1]) for e in evs] for i in range(npass)]
+    pass_ms = [[e[i].elapsed_time(e[i + 1]) for e in evs] for i in range(nlaunch)]
     total_ms = sum(step_ms)
     if world > 1:
         t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     ms = total_ms / args.steps
-    fl = flops_of(shape, wl["kind"])
+    fl = flops_of(shape, wl["kind"]) * len(ops)
     value = fl * world / (ms * 1e-3) / 1e9
 
     peak, peak_kind = load_peaks()
     bytes_pass = 2.0 * nelem * elem  # one compulsory read + write of the array per pass
     avg_pass = [sum(p) / len(p) for p in pass_ms]
-    dom = max(range(npass), key=lambda i: avg_pass[i]) if npass else 0
-    ach = bytes_pass / (avg_pass[dom] * 1e-3) / 1e9 if npass else 0.0
-    ach_tr = bytes_pass / (ms * 1e-3) / 1e9
+    dom = max(range(nlaunch), key=lambda i: avg_pass[i]) if nlaunch else 0
+    ach = bytes_pass / (avg_pass[dom] * 1e-3) / 1e9 if nlaunch else 0.0
+    ach_tr = bytes_pass * len(ops) / (ms * 1e-3) / 1e9
 
     # accuracy of one result vs FP64 (numpy pocketfft), outside the timed region
     rel_err = None
+    roundtrip_err = None
     ref = None
     if rank == 0 and not args.no_check:
         one_step()
@@ -326,8 +350,11 @@ def run_gbfft(args, wl):
         yy = y.cpu().numpy().astype(np.complex128)
         xx = x_cpu.numpy().astype(np.complex128)
         axes = tuple(range(len(shape))) if wl["kind"] == "full" else (-1,)
-        ref = np.fft.fftn(xx, axes=axes) if wl["mode"] == "forward" else np.fft.ifftn(xx, axes=axes)
+        ref = np.fft.fftn(xx, axes=axes) if step_modes(wl)[0] == "forward" else np.fft.ifftn(xx, axes=axes)
         rel_err = float(np.linalg.norm(yy - ref) / np.linalg.norm(ref))
+        if len(ops) > 1:  # Inverse(Forward(x)) against x
+            zz = z.cpu().numpy().astype(np.complex128)
+            roundtrip_err = float(np.linalg.norm(zz - xx) / np.linalg.norm(xx))
 
     # the other precision of the same transform (split-FP16 tensor-core rows vs
     # plain FP32), timed the same way, with its own error vs FP64
@@ -341,6 +368,7 @@ def run_gbfft(args, wl):
         except Exception as exc:  # the planner rejects shapes it has no kernel for
             other_prec = {"precision": other, "unavailable": str(exc)}
         else:
+            mode = modes[0]
             for _ in range(max(3, args.warmup)):
                 L.check(lib.gbfft_exec(p2.handle, mode, ctypes.c_void_p(x.data_ptr()),
                                        ctypes.c_void_p(y.data_ptr()), sp))
@@ -359,47 +387,55 @@ def run_gbfft(args, wl):
             if ref is not None:
                 yy2 = y.cpu().numpy().astype(np.complex128)
                 err2 = float(np.linalg.norm(yy2 - ref) / np.linalg.norm(ref))
-            other_prec = {"precision": other, "ms_per_step": ms2,
-                          "value": fl * world / (ms2 * 1e-3) / 1e9, "unit": "GFLOP/s",
+            other_prec = {"precision": other, "ms_per_step": ms2, "transforms": 1,
+                          "value": flops_of(shape, wl["kind"]) * world / (ms2 * 1e-3) / 1e9, "unit": "GFLOP/s",
                           "rel_err_vs_fp64": err2, "speedup_of_split_fp16_over_fp32":
-                              (ms / ms2) if other == "split_fp16" else (ms2 / ms),
+                              (ms / len(ops) / ms2) if other == "split_fp16" else (ms2 * len(ops) / ms),
                           "kernels": p2.pass_kernels()}
             p2.close()
 
     # end to end through the C ABI with host buffers (pinned): every step
-    # copies its input host -> device, executes and copies the result back.
-    # Single stream: one step at a time.  Pipelined: steps alternate between
-    # two streams with their own buffers, so one step's host -> device copy
-    # overlaps the previous step's device -> host copy (the link is full
-    # duplex) and its transform.
+    # copies its input host -> device, runs its transforms and copies the
+    # result back.  Single stream: one step at a time.  Pipelined: steps
+    # rotate over NS streams with their own buffers, so one step's
+    # host -> device copy overlaps another's device -> host copy (the link is
+    # full duplex) and the transforms.
+    NS = 3
     hx = x_cpu.pin_memory()
-    hy = [torch.empty_like(hx).pin_memory() for _ in range(2)]
+    hy = [torch.empty_like(hx).pin_memory() for _ in range(NS)]
+
+    def run_ops(bufs, st_ptr):
+        # bufs: (input, intermediate, output) device buffers of one step
+        for j, (m, _a, _b) in enumerate(ops):
+            a = bufs[0] if j == 0 else bufs[1]
+            b = bufs[1] if j == 0 and len(ops) > 1 else bufs[2]
+            L.check(lib.gbfft_exec(plan.handle, m, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()),
+                                   st_ptr))
+
     e2e_ms = []
     for k in range(max(3, min(args.steps, 20)) + 2):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         x.copy_(hx, non_blocking=True)
-        L.check(lib.gbfft_exec(plan.handle, mode, ctypes.c_void_p(x.data_ptr()),
-                               ctypes.c_void_p(y.data_ptr()), sp))
-        hy[0].copy_(y, non_blocking=True)
+        run_ops((x, y, result), sp)
+        hy[0].copy_(result, non_blocking=True)
         e1.record(stream)
         torch.cuda.synchronize()
         if k >= 2:
             e2e_ms.append(e0.elapsed_time(e1))
     e2e_single = statistics.mean(e2e_ms)
-    streams2 = [torch.cuda.Stream(dev) for _ in range(2)]
-    xb = [x, torch.empty_like(x)]
-    yb = [y, torch.empty_like(y)]
-    n_pipe = max(4, min(args.steps, 20))
+    streamsN = [torch.cuda.Stream(dev) for _ in range(NS)]
+    bufsN = [(torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)) for _ in range(NS)]
+    n_pipe = max(6, min(args.steps, 20))
 
     def pipelined(nsteps):
         for k in range(nsteps):
-            st = streams2[k % 2]
+            st = streamsN[k % NS]
+            bx, bm, bo = bufsN[k % NS]
             with torch.cuda.stream(st):
-                xb[k % 2].copy_(hx, non_blocking=True)
-                L.check(lib.gbfft_exec(plan.handle, mode, ctypes.c_void_p(xb[k % 2].data_ptr()),
-                                       ctypes.c_void_p(yb[k % 2].data_ptr()), ctypes.c_void_p(st.cuda_stream)))
-                hy[k % 2].copy_(yb[k % 2], non_blocking=True)
+                bx.copy_(hx, non_blocking=True)
+                run_ops((bx, bm, bo), ctypes.c_void_p(st.cuda_stream))
+                hy[k % NS].copy_(bo, non_blocking=True)
 
     pipelined(2)
     torch.cuda.synchronize()
@@ -413,7 +449,9 @@ def run_gbfft(args, wl):
     # cuFFT on the same input and timing (comparator only, not the product)
     cufft_ms = None
     if rank == 0 and not args.no_cufft:
-        f = (lambda t: torch.fft.fftn(t)) if wl["kind"] == "full" else (lambda t: torch.fft.fft(t, dim=-1))
+        f1 = (lambda t: torch.fft.fftn(t)) if wl["kind"] == "full" else (lambda t: torch.fft.fft(t, dim=-1))
+        fi = (lambda t: torch.fft.ifftn(t)) if wl["kind"] == "full" else (lambda t: torch.fft.ifft(t, dim=-1))
+        f = (lambda t: fi(f1(t))) if len(ops) > 1 else f1
         for _ in range(3):
             f(x)
         ts = []
@@ -441,7 +479,8 @@ def run_gbfft(args, wl):
                        "precision": args.precision, "seed": 1234,
                        "l2": "flushed (256 MiB write) between timed steps; working set 2x%d MiB"
                              % (nelem * elem >> 20),
-                       "plan": plan.describe(), "parallelism": "replicas" if world > 1 else "single",
+                       "plan": plan.describe(), "transforms_per_step": len(ops),
+                       "parallelism": "replicas" if world > 1 else "single",
                        "autotune": tune_report.strip().splitlines()[-1] if tune_report else "off"},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                          "frac": ach / peak,
@@ -453,13 +492,14 @@ def run_gbfft(args, wl):
             "roofline_transform": {"achieved": ach_tr, "frac": ach_tr / peak, "kernels": kernels,
                                    "bytes_alg": bytes_pass, "pass_ms": avg_pass},
             "rel_err_vs_fp64": rel_err,
+            "roundtrip_rel_err": roundtrip_err,
             "other_precision": other_prec,
             "e2e": {"value": e2e, "unit": "GFLOP/s", "h2d_bytes_per_step": nelem * elem,
                     "d2h_bytes_per_step": nelem * elem, "ms_per_step": e2e_best,
-                    "ms_per_step_single_stream": e2e_single, "ms_per_step_two_streams": e2e_pipe,
-                    "timing": "single stream: CUDA events per step; two streams: host wall clock over "
-                              "%d steps between device synchronisations" % n_pipe},
-            "gpu_launches": args.steps * npass,
+                    "ms_per_step_single_stream": e2e_single, "ms_per_step_pipelined": e2e_pipe,
+                    "timing": "single stream: CUDA events per step; pipelined over %d streams: host wall "
+                              "clock over %d steps between device synchronisations" % (NS, n_pipe)},
+            "gpu_launches": args.steps * nlaunch,
             "clocks": clocks,
             "cufft_comparator_ms": cufft_ms,
             "cpu_baseline": cpu,
