@@ -425,6 +425,16 @@ static bool split_four_step(int64_t n, int cap, int64_t& n1, int64_t& n2, bool d
   return true;
 }
 
+// "16.16.8": the stage radices of a pass, for plan descriptions.
+static std::string radix_list(const PassDesc& d) {
+  std::string r;
+  for (int i = 0; i < d.nstages; ++i) {
+    if (i) r += '.';
+    r += std::to_string(d.st[i].radix);
+  }
+  return r;
+}
+
 // Appends the passes of one axis.  `first`: this axis reads the user's
 // input; later axes work on the output buffer.
 int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
@@ -471,8 +481,8 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     ps.src = src;
     ps.dst = R_OUT;
     passes.push_back(ps);
-    std::snprintf(buf, sizeof buf, "[n=%lld es=%lld %s W=%d]", (long long)ax.n, (long long)ax.es,
-                  kname, ps.d.W);
+    std::snprintf(buf, sizeof buf, "[n=%lld r=%s es=%lld %s W=%d]", (long long)ax.n, radix_list(ps.d).c_str(),
+                  (long long)ax.es, kname, ps.d.W);
     desc += buf;
     return GBFFT_OK;
   }

@@ -47,7 +47,7 @@ def test_planner_choices(gbfft_lib):
     st, s = explain((4096, 4096))
     assert st == 0 and "launches=2" in s and "scratch=0" in s
     st, s = explain((65536, 1000), kind=0)
-    assert st == 0 and "[n=1000 es=1" in s and "launches=1" in s
+    assert st == 0 and "[n=1000 r=10.10.10 es=1 row" in s and "launches=1" in s
     st, s = explain((4096, 1009), kind=0)
     assert st == 0 and "bluestein m=2048" in s and "launches=1" in s
     st, s = explain((65536,))
@@ -60,6 +60,18 @@ def test_planner_choices(gbfft_lib):
     assert st == 0 and "launches=3" in s
     st, s = explain((1, 1, 1))
     assert st == 0 and "launches=0" in s
+
+
+@pytest.mark.parametrize("n,radices", [(4096, "16.16.16"), (2048, "16.16.8"), (512, "16.16.2"),
+                                       (243, "9.9.3"), (250, "10.5.5"), (210, "15.14"), (189, "9.7.3"),
+                                       (105, "15.7"), (343, "7.7.7"), (2025, "15.15.9"), (12, "12"),
+                                       (6, "6"), (3 * 2048, "16.16.12.2")])
+def test_stage_radices(gbfft_lib, n, radices):
+    """Powers of two keep radix 16 then 8/4/2 (the register kernels' lists);
+    lengths with odd factors take the fewest stages over radices up to 16,
+    composite 6/9/10/12/14/15 included, larger radices first."""
+    st, s = explain((4, n), kind=0)
+    assert st == 0 and ("r=%s " % radices) in s, s
 
 
 def test_planner_rejects_bad_arguments(gbfft_lib):
