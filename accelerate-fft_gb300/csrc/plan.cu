@@ -600,7 +600,7 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
                                  bluestein_multipass_length(ax.n, cap, dbl,
                                                             blue_pad > 0    ? 2.5
                                                             : blue_pad == 0 ? 1.0
-                                                                            : kRaggedGenericWeight),
+                                                                            : tc->blue_weight),
                                  cap, split_rank,
                                  scratch1, scratch2, desc);
 }

@@ -70,6 +70,7 @@ struct TuneChoice {
   int blue_pad = 1;     // Bluestein padding: 1 power of two when cheaper, 0 smallest smooth m,
                         //   -1 the ragged executor's weighting
   int row_kernel = -1;  // contiguous rows: 1 register row kernel, 0 generic tile, -1 by rule
+  double blue_weight = 2.0;  // with blue_pad -1: the ragged executor's generic-tile weight
   bool tuned = false;   // set by the autotuner (or its cache)
 };
 
@@ -78,10 +79,17 @@ bool factor_device(int64_t n, std::vector<int>& out);
 bool is_fast_length(int64_t n);
 int64_t bluestein_length(int64_t n);
 int64_t bluestein_multipass_length(int64_t n, int cap, bool dbl, double generic);
-// Relative per-element cost of a generic-tile four-step half inside the
-// ragged executor (its strided tiles load directly, so the gap to the
-// register tiles is smaller than in plans); TuneChoice::blue_pad = -1.
-constexpr double kRaggedGenericWeight = 2.0;
+// Ragged-executor choices the autotuner searches over.
+struct RaggedTune {
+  int budget = 0;            // elements per tile and single-tile length cap (0: 4096, 2048 for C64)
+  double blue_weight = 2.0;  // generic-tile weight when choosing multi-pass Bluestein lengths
+                             // (its strided tiles load directly, so the gap to the generic
+                             // tile is smaller than in plans, where it is 2.5)
+  int strided = 1;           // register strided tiles for power-of-two four-step halves
+  bool tuned = false;
+};
+std::string tune_device_tag();  // "<device name> sm_XY <n>SM" of the current device
+
 void blue_tables(int64_t n, int64_t m, std::vector<cd>& chirp, std::vector<cd>& filter);
 void host_fft_fp64(std::vector<cd>& x);
 void choose_tile(PassSpec& ps, bool dbl);

@@ -25,6 +25,8 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "gbfft.h"
@@ -188,17 +190,26 @@ struct gbfft_ragged_plan {
   RaggedArgs args{};
   // per-transform comparator: one ordinary plan per distinct length
   std::map<int64_t, gbfft_plan*> len_plans;
+  gbfft::RaggedTune tune;  // the choices the plan was built with
 };
+
+namespace gbfft {
+int create_ragged(gbfft_ragged_plan** out, int64_t count, const int64_t* lengths, const int64_t* offsets,
+                  const int* modes, int dtype, const RaggedTune* forced);
+int autotune_ragged(int64_t count, const int64_t* lengths, const int64_t* offsets, const int* modes, int dtype,
+                    void* stream, RaggedTune& best, std::string* report);
+}  // namespace gbfft
 
 namespace {
 
 // Tile width for a ragged pass: at most `budget` elements per tile.  Strided
 // halves whose length has a register kernel use it with W = 4096 / n.
-void ragged_tile(PassSpec& ps, bool dbl, int budget, int64_t group) {
+void ragged_tile(PassSpec& ps, bool dbl, int budget, int64_t group, bool strided) {
   PassDesc& d = ps.d;
   const int n = d.n;
-  if (group == 0 && d.in_cs == 1 && d.in_es != 1 && (n == 64 || n == 128 || n == 256 || n == 512 || n == 1024) &&
-      str_ops_supported(d.flags) && !feature_disabled("strided")) {
+  if (strided && group == 0 && d.in_cs == 1 && d.in_es != 1 &&
+      (n == 64 || n == 128 || n == 256 || n == 512 || n == 1024) && str_ops_supported(d.flags) &&
+      !feature_disabled("strided")) {
     d.kernel = K_STRIDED;
     d.W = 4096 / n;
     d.threads = kRaggedThreads;
@@ -240,6 +251,48 @@ extern "C" {
 
 int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64_t* lengths,
                              const int64_t* offsets, const int* modes, int dtype) {
+  return gbfft::create_ragged(out, count, lengths, offsets, modes, dtype, nullptr);
+}
+
+int gbfft_ragged_autotune(int64_t count, const int64_t* lengths, const int64_t* offsets, const int* modes,
+                          int dtype, void* stream, char* report, size_t cap) {
+  gbfft::RaggedTune best;
+  std::string rep;
+  const int st = gbfft::autotune_ragged(count, lengths, offsets, modes, dtype, stream, best, &rep);
+  if (report && cap) std::snprintf(report, cap, "%s", rep.c_str());
+  return st;
+}
+
+}  // extern "C"
+
+namespace gbfft {
+
+namespace {
+std::mutex g_rtune_mu;
+std::map<std::string, RaggedTune> g_rtune;
+
+// device + FNV-1a hash of the lengths and modes (the offsets do not change
+// the work)
+std::string ragged_key(int64_t count, const int64_t* lengths, const int* modes, int dtype) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](uint64_t v) {
+    for (int i = 0; i < 8; ++i) {
+      h ^= (v >> (8 * i)) & 0xFF;
+      h *= 1099511628211ull;
+    }
+  };
+  for (int64_t i = 0; i < count; ++i) {
+    mix(uint64_t(lengths[i]));
+    mix(uint64_t(uint32_t(modes[i])));
+  }
+  char b[96];
+  std::snprintf(b, sizeof b, "|ragged|%lld|%d|%016llx", (long long)count, dtype, (unsigned long long)h);
+  return tune_device_tag() + b;
+}
+}  // namespace
+
+int create_ragged(gbfft_ragged_plan** out, int64_t count, const int64_t* lengths, const int64_t* offsets,
+                  const int* modes, int dtype, const RaggedTune* forced) {
   if (!out) return GBFFT_ERR_INVALID_ARG;
   *out = nullptr;
   if (count < 0 || (count > 0 && (!lengths || !modes))) return GBFFT_ERR_INVALID_ARG;
@@ -264,8 +317,31 @@ int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64
   if (cudaGetDevice(&p->device) != cudaSuccess) return GBFFT_ERR_CUDA;
   if (prepare_kernels() != cudaSuccess) return GBFFT_ERR_CUDA;
   const bool dbl = p->dbl;
-  const int budget = dbl ? 2048 : 4096;
+  RaggedTune rt;
+  if (forced) {
+    rt = *forced;
+  } else if (count > 0) {
+    const std::string key = ragged_key(count, lengths, modes, dtype);
+    bool hit = false;
+    {
+      std::lock_guard<std::mutex> lk(g_rtune_mu);
+      auto it = g_rtune.find(key);
+      if (it != g_rtune.end()) {
+        rt = it->second;
+        hit = true;
+      }
+    }
+    if (!hit) {
+      if (const char* at = std::getenv("GBFFT_AUTOTUNE"); at && at[0] == '1') {
+        RaggedTune best;
+        if (autotune_ragged(count, lengths, offsets, modes, dtype, nullptr, best, nullptr) == GBFFT_OK) rt = best;
+      }
+    }
+  }
+  p->tune = rt;
+  const int budget = rt.budget > 0 ? rt.budget : (dbl ? 2048 : 4096);
   const int cap = budget;  // single-tile lengths; longer ones go four-step
+  const bool strided = rt.strided != 0;
 
   // ---- pass templates per distinct length -------------------------------
   Builder B;
@@ -283,7 +359,7 @@ int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64
       if (lengths[i] <= 1 || is_fast_length(lengths[i])) continue;
       // the padded length add_axis will pick (single tile, or four-pass)
       int64_t m = bluestein_length(lengths[i]);
-      if (m > cap) m = bluestein_multipass_length(lengths[i], cap, dbl, kRaggedGenericWeight);
+      if (m > cap) m = bluestein_multipass_length(lengths[i], cap, dbl, rt.blue_weight);
       nm.push_back({lengths[i], m});
     }
     B.precompute_blue(nm);
@@ -297,6 +373,7 @@ int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64
     const Axis ax{n, 1, n, 1, n, 1};
     TuneChoice rc;
     rc.blue_pad = -1;  // the ragged executor's Bluestein weighting
+    rc.blue_weight = rt.blue_weight;
     const int st = add_axis(B, lc.passes, ax, true, s1, s2, desc, cap, &rc);
     if (st != GBFFT_OK) return st;
     lc.m = s2;  // rows (1) * m for the four-pass Bluestein, else 0
@@ -344,7 +421,7 @@ int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64
     if (n == 1) continue;  // filled by the copy below
     const PassSpec& base = classes[n].passes[0];
     PassSpec ps = base;
-    ragged_tile(ps, dbl, budget, int64_t(kv.second.size()));
+    ragged_tile(ps, dbl, budget, int64_t(kv.second.size()), strided);
     const int W = ps.d.W;
     const int di = int(descs.size());
     descs.push_back(ps);
@@ -384,7 +461,7 @@ int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64
       auto it = desc_index.find(key);
       if (it == desc_index.end()) {
         PassSpec ps = lc.passes[size_t(k)];
-        ragged_tile(ps, dbl, budget, 0);
+        ragged_tile(ps, dbl, budget, 0, strided);
         it = desc_index.emplace(key, int(descs.size())).first;
         descs.push_back(ps);
       }
@@ -486,6 +563,10 @@ int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64
   *out = p.release();
   return GBFFT_OK;
 }
+
+}  // namespace gbfft
+
+extern "C" {
 
 int gbfft_ragged_plan_destroy(gbfft_ragged_plan* plan) {
   destroy_ragged(plan);
@@ -591,3 +672,116 @@ int gbfft_ragged_status(const gbfft_ragged_plan* p, void* stream) {
 }
 
 }  // extern "C"
+
+namespace gbfft {
+
+// Times candidate ragged plans (tile budget, Bluestein length weighting,
+// register strided tiles) on scratch buffers and keeps the fastest per
+// (device, lengths, modes); coordinate descent from the defaults, one
+// untimed and three timed launches per candidate (CUDA events, median).
+int autotune_ragged(int64_t count, const int64_t* lengths, const int64_t* offsets, const int* modes, int dtype,
+                    void* stream, RaggedTune& best, std::string* report) {
+  if (count <= 0 || !lengths || !modes) return GBFFT_ERR_INVALID_ARG;
+  const bool dbl = dtype == GBFFT_C64;
+  const size_t eb = dbl ? 16 : 8;
+  int64_t total = 0, run = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    const int64_t o = offsets ? offsets[i] : run;
+    total = std::max(total, o + lengths[i]);
+    run += lengths[i];
+  }
+  best = RaggedTune{};
+  if (total == 0) return GBFFT_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void *din = nullptr, *dout = nullptr;
+  if (cudaMalloc(&din, size_t(total) * eb) != cudaSuccess) return GBFFT_ERR_ALLOC;
+  if (cudaMalloc(&dout, size_t(total) * eb) != cudaSuccess) {
+    cudaFree(din);
+    return GBFFT_ERR_ALLOC;
+  }
+  cudaMemsetAsync(din, 0, size_t(total) * eb, s);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto time_one = [&](const RaggedTune& c, double& ms) -> int {
+    gbfft_ragged_plan* p = nullptr;
+    int st = create_ragged(&p, count, lengths, offsets, modes, dtype, &c);
+    if (st != GBFFT_OK) return st;
+    std::vector<float> t;
+    for (int i = 0; i < 4 && st == GBFFT_OK; ++i) {
+      cudaEventRecord(e0, s);
+      st = gbfft_ragged_exec(p, din, dout, s);
+      cudaEventRecord(e1, s);
+      if (cudaEventSynchronize(e1) != cudaSuccess) st = GBFFT_ERR_CUDA;
+      float x = 0;
+      cudaEventElapsedTime(&x, e0, e1);
+      if (i > 0) t.push_back(x);
+    }
+    if (st == GBFFT_OK) st = gbfft_ragged_status(p, stream);
+    gbfft_ragged_plan_destroy(p);
+    if (st != GBFFT_OK) return st;
+    std::sort(t.begin(), t.end());
+    ms = t[t.size() / 2];
+    return GBFFT_OK;
+  };
+  auto line = [&](const RaggedTune& c, double ms) {
+    if (!report) return;
+    char b[128];
+    std::snprintf(b, sizeof b, "budget=%d blue_weight=%.1f strided=%d: %.4f ms\n",
+                  c.budget > 0 ? c.budget : (dbl ? 2048 : 4096), c.blue_weight, c.strided, ms);
+    *report += b;
+  };
+  double best_ms = 0;
+  int st = time_one(best, best_ms);
+  if (st == GBFFT_OK) {
+    line(best, best_ms);
+    const int b0 = dbl ? 2048 : 4096;
+    const std::vector<int> budgets = {b0, b0 / 2};
+    const std::vector<double> weights = {2.0, 1.0, 3.0};
+    const std::vector<int> strides = {1, 0};
+    for (int knob = 0; knob < 3 && st == GBFFT_OK; ++knob) {
+      const RaggedTune start = best;
+      const size_t nv = knob == 0 ? budgets.size() : knob == 1 ? weights.size() : strides.size();
+      for (size_t v = 0; v < nv; ++v) {
+        RaggedTune c = start;
+        if (knob == 0) {
+          if (budgets[v] == (start.budget > 0 ? start.budget : b0)) continue;
+          c.budget = budgets[v];
+        } else if (knob == 1) {
+          if (weights[v] == start.blue_weight) continue;
+          c.blue_weight = weights[v];
+        } else {
+          if (strides[v] == start.strided) continue;
+          c.strided = strides[v];
+        }
+        double ms = 0;
+        st = time_one(c, ms);
+        if (st != GBFFT_OK) break;
+        line(c, ms);
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = c;
+        }
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(din);
+  cudaFree(dout);
+  if (st != GBFFT_OK) return st;
+  best.tuned = true;
+  {
+    std::lock_guard<std::mutex> lk(g_rtune_mu);
+    g_rtune[ragged_key(count, lengths, modes, dtype)] = best;
+  }
+  if (report) {
+    char b[128];
+    std::snprintf(b, sizeof b, "best: budget=%d blue_weight=%.1f strided=%d %.4f ms\n",
+                  best.budget > 0 ? best.budget : (dbl ? 2048 : 4096), best.blue_weight, best.strided, best_ms);
+    *report += b;
+  }
+  return GBFFT_OK;
+}
+
+}  // namespace gbfft

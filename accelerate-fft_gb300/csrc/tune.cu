@@ -132,6 +132,8 @@ bool has_flag(const gbfft_plan* p, uint32_t flag) {
 
 }  // namespace
 
+std::string tune_device_tag() { return device_tag(); }
+
 std::string tune_key(int rank, const int64_t* dims, int kind, int dtype, int precision) {
   std::string k = device_tag();
   char b[64];

@@ -7,4 +7,4 @@ served by libgbfft.so through its C ABI (include/gbfft.h).
 """
 from ._lib import GbfftError, lib, error_string  # noqa: F401
 from .fft import (Mode, Plan, RaggedPlan, SpecConvPlan, autotune, fft, fft1D, fft2D,  # noqa: F401
-                  fft3D, mode_code)
+                  fft3D, mode_code, ragged_autotune)

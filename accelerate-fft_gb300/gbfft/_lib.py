@@ -52,6 +52,7 @@ SIGNATURES = {
     "gbfft_plan_explain": (_i, [_i, _i64p, _i, _i, _i, ctypes.c_char_p, _sz]),
     "gbfft_ragged_plan_create": (_i, [ctypes.POINTER(_vp), _i64, _i64p, _i64p,
                                       ctypes.POINTER(_i), _i]),
+    "gbfft_ragged_autotune": (_i, [_i64, _i64p, _i64p, ctypes.POINTER(_i), _i, _vp, ctypes.c_char_p, _sz]),
     "gbfft_ragged_exec": (_i, [_vp, _vp, _vp, _vp]),
     "gbfft_ragged_exec_per_transform": (_i, [_vp, _vp, _vp, _vp]),
     "gbfft_ragged_plan_destroy": (_i, [_vp]),

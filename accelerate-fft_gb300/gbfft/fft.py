@@ -173,6 +173,24 @@ def fft3D(mode, arr, stream=None):
     return _run(L.KIND_FULL, mode, arr, stream)
 
 
+def ragged_autotune(lengths, modes, offsets=None, dtype=torch.complex64, stream=None):
+    """Times candidate ragged plans for these lengths and modes
+    (gbfft_ragged_autotune) and caches the fastest; returns the report."""
+    import numpy as np
+    lengths = np.ascontiguousarray(np.asarray(lengths, dtype=np.int64))
+    modes = np.ascontiguousarray(np.asarray([mode_code(m) for m in modes], dtype=np.int32))
+    off = None
+    if offsets is not None:
+        offsets = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
+        off = offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    buf = ctypes.create_string_buffer(8192)
+    L.check(L.lib().gbfft_ragged_autotune(len(lengths), lengths.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                          off, modes.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                          L.C64 if dtype == torch.complex128 else L.C32, _stream(stream),
+                                          buf, 8192), "gbfft_ragged_autotune")
+    return buf.value.decode()
+
+
 class RaggedPlan:
     """Many 1D transforms of uneven lengths and modes over one flat buffer,
     run by one persistent launch (gbfft_ragged_plan_create / _exec)."""

@@ -529,6 +529,10 @@ def run_ragged(args, wl):
     x_cpu = torch.complex(torch.randn(total, generator=g), torch.randn(total, generator=g))
     x = x_cpu.to(dev)
     y = torch.empty_like(x)
+    tune_report = None
+    if not args.no_tune:
+        # plan creation with the autotuner (untimed, like any plan creation)
+        tune_report = gbfft.ragged_autotune(lengths, modes)
     t0 = time.perf_counter()
     plan = gbfft.RaggedPlan(lengths, modes)
     plan_s = time.perf_counter() - t0
@@ -610,6 +614,7 @@ def run_ragged(args, wl):
             "config": {"workload": wl["desc"], "count": int(len(lengths)), "elements": total,
                        "seed": 4, "l2": "flushed (256 MiB write) between timed steps; working set "
                        "2x%d MiB" % (total * 8 >> 20), "plan_seconds": plan_s,
+                       "autotune": tune_report.strip().splitlines()[-1] if tune_report else "off",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                          "frac": ach / peak, "traffic": ncu_traffic(args.workload, "ragged_kernel"),

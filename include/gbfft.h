@@ -162,6 +162,15 @@ int gbfft_tune_count(void);
 typedef struct gbfft_ragged_plan gbfft_ragged_plan;
 int gbfft_ragged_plan_create(gbfft_ragged_plan** out, int64_t count, const int64_t* lengths,
                              const int64_t* offsets, const int* modes, int dtype);
+
+/* Autotuner for a ragged batch (new): times candidate plans of these
+ * lengths and modes (tile budget, Bluestein padded-length weighting,
+ * register strided tiles) on scratch buffers on `stream` and caches the
+ * fastest per (device, lengths, modes); later gbfft_ragged_plan_create calls
+ * for the same batch use it (GBFFT_AUTOTUNE=1 makes plan creation tune on a
+ * miss).  `report` (may be NULL) receives one line per candidate. */
+int gbfft_ragged_autotune(int64_t count, const int64_t* lengths, const int64_t* offsets, const int* modes,
+                          int dtype, void* stream, char* report, size_t cap);
 int gbfft_ragged_exec(const gbfft_ragged_plan* plan, const void* d_in, void* d_out, void* stream);
 /* The same transforms issued as one launch sequence per transform (the
  * "one launch per transform" comparator). */

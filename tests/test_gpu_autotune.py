@@ -61,3 +61,30 @@ def test_autotune_on_plan_creation(clean_tuner, monkeypatch):
     rng = np.random.default_rng(32)
     assert "tuned(" in check_plan(g, (512, 4096), "full", rng)
     assert clean_tuner.gbfft_tune_count() == 1
+
+
+def test_ragged_autotune(gbfft_lib):
+    """The ragged search runs, caches a choice that the next plan of the same
+    batch uses, and the tuned plan stays correct against FP64."""
+    g = gbfft_lib
+    from gbfft import synth
+    lengths, modes = synth.ragged_lengths(300, seed=11)
+    report = g.ragged_autotune(lengths, modes)
+    lines = [ln for ln in report.splitlines() if ln.strip()]
+    assert len(lines) >= 4 and lines[-1].startswith("best:"), report
+    plan = g.RaggedPlan(lengths, modes)
+    total = int(lengths.sum())
+    rng = np.random.default_rng(12)
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    xt = torch.from_numpy(x).cuda()
+    y = torch.empty_like(xt)
+    plan.exec_ptr(xt.data_ptr(), y.data_ptr())
+    torch.cuda.synchronize()
+    assert plan.status() == 0
+    yy = y.cpu().numpy()
+    for i in range(0, len(lengths), 7):
+        n, o = int(lengths[i]), int(plan.offsets[i])
+        r = np.fft.fft(x[o:o + n].astype(np.complex128)) if modes[i] == -1 else \
+            np.fft.ifft(x[o:o + n].astype(np.complex128))
+        assert rel_l2(yy[o:o + n], r) < 4e-6, (i, n)
+    plan.close()
