@@ -100,6 +100,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(ms, world, device):
+    """The slowest rank's time: replicas run in parallel, so the job takes as
+    long as its slowest rank (a no-op for one process)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, world, ms):
+    """Whole-job rate: the units every rank processed over the slowest rank's
+    time (weak scaling: each rank runs the full workload)."""
+    return units_per_rank * world / (ms * 1e-3) / 1e9
+
+
 def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -324,14 +342,10 @@ def run_gbfft(args, wl):
     clocks = sampler.stop() if sampler else None
     step_ms = [e[0].elapsed_time(e[-1]) for e in evs]
     pass_ms = [[e[i].elapsed_time(e[i + 1]) for e in evs] for i in range(nlaunch)]
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), world, dev)
     ms = total_ms / args.steps
     fl = flops_of(shape, wl["kind"]) * len(ops)
-    value = fl * world / (ms * 1e-3) / 1e9
+    value = job_throughput(fl, world, ms)
 
     peak, peak_kind = load_peaks()
     bytes_pass = 2.0 * nelem * elem  # one compulsory read + write of the array per pass
@@ -566,13 +580,9 @@ def run_ragged(args, wl):
     if world > 1:
         torch.distributed.barrier()
     clocks = sampler.stop() if sampler else None
-    ms = sum(ts) / len(ts)
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(ts) / len(ts), world, dev)
     status = plan.status()
-    value = fl * world / (ms * 1e-3) / 1e9
+    value = job_throughput(fl, world, ms)
     peak, peak_kind = load_peaks()
     ach = bytes_alg / (ms * 1e-3) / 1e9
     per_ms = statistics.mean(timed(True, 3, 1)) if rank == 0 and not args.no_compare else None
@@ -719,12 +729,8 @@ def run_specconv(args, wl):
     clocks = sampler.stop() if sampler else None
     fwd = [e[0].elapsed_time(e[1]) for e in evs]
     bwd = [e[1].elapsed_time(e[2]) for e in evs]
-    ms = (sum(fwd) + sum(bwd)) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = fl * world / (ms * 1e-3) / 1e9
+    ms = max_over_ranks((sum(fwd) + sum(bwd)) / args.steps, world, dev)
+    value = job_throughput(fl, world, ms)
     peak, peak_kind = load_peaks()
     # algorithmic bytes: fwd reads x, H and writes y; adjoint reads x, g_y, H and writes g_x, g_H
     fb = (2 * x.numel() + H.numel()) * 8.0
