@@ -78,7 +78,7 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
 // one kind does not inflate the others.
 template <typename T, int N, int W, int... Rs>
 __device__ __noinline__ void ragged_str(const PassDesc& d, int64_t tile, unsigned char* smem) {
-  str_tile_dispatch<T, N, W, Rs...>(d, tile, smem);
+  str_tile_dispatch_ragged<T, N, W, Rs...>(d, tile, smem);
 }
 template <typename T>
 __device__ __noinline__ void ragged_pencil(const PassDesc& d, int64_t tile, unsigned char* smem) {
@@ -208,7 +208,7 @@ void ragged_tile(PassSpec& ps, bool dbl, int budget, int64_t group, bool strided
   PassDesc& d = ps.d;
   const int n = d.n;
   if (strided && group == 0 && d.in_cs == 1 && d.in_es != 1 &&
-      (n == 64 || n == 128 || n == 256 || n == 512 || n == 1024) && str_ops_supported(d.flags) &&
+      (n == 64 || n == 128 || n == 256 || n == 512 || n == 1024) && str_ops_ragged(d.flags & kStrOpMask) &&
       !feature_disabled("strided")) {
     d.kernel = K_STRIDED;
     d.W = 4096 / n;

@@ -600,7 +600,7 @@ struct RowCfg {
   static constexpr int threads = ROWS * (N / E);
   static constexpr bool tma_capable = sizeof(T) == 4 && N % 16 == 0;
   static size_t smem() { return size_t(2) * ROWS * row_pitch<N>() * sizeof(typename CxT<T>::type); }
-  static int tma_ctas_per_sm;
+  [[maybe_unused]] static int tma_ctas_per_sm;
   static constexpr int MINB1 = (MINB >= 3 && sizeof(T) == 4) ? 4 : MINB;
   static cudaError_t prepare() {
     cudaError_t e = cudaFuncSetAttribute(rowfft_kernel<T, N, E, ROWS, MINB, Rs...>,

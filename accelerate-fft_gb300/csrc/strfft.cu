@@ -209,7 +209,7 @@ struct StrCfg {
   static size_t smem() { return size_t(N) * W * sizeof(typename CxT<T>::type); }
   // tensor-fed kernel: alignment slack, two tile buffers, two mbarriers
   static size_t tma_smem() { return 128 + 2 * smem() + 2 * sizeof(uint64_t); }
-  static inline int tma_ctas[7] = {0, 0, 0, 0, 0, 0, 0};  // resident CTAs per SM of each tensor-fed kernel
+  [[maybe_unused]] static inline int tma_ctas[7] = {0, 0, 0, 0, 0, 0, 0};  // resident CTAs per SM, tensor-fed
   template <uint32_t OPS>
   static cudaError_t prep1() {
     cudaError_t e = cudaFuncSetAttribute(strfft_kernel<T, N, W, MINB, OPS, Rs...>,

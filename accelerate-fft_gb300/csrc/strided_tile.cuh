@@ -413,6 +413,23 @@ __device__ __forceinline__ bool str_tile_dispatch(const PassDesc& d, int64_t til
   }
 }
 
+// The sets the ragged executor generates (four-step halves, multi-pass
+// Bluestein): only these are instantiated inside its persistent kernel.
+__host__ __device__ constexpr bool str_ops_ragged(uint32_t ops) {
+  return ops == SO_PLAIN || ops == SO_TW4 || ops == SO_BP1 || ops == SO_BMID || ops == SO_COUT;
+}
+template <typename T, int N, int W, int... Rs>
+__device__ __forceinline__ bool str_tile_dispatch_ragged(const PassDesc& d, int64_t tile, unsigned char* smem) {
+  switch (d.flags & kStrOpMask) {
+    case SO_PLAIN: str_tile<T, N, W, SO_PLAIN, Rs...>(d, tile, smem); return true;
+    case SO_TW4: str_tile<T, N, W, SO_TW4, Rs...>(d, tile, smem); return true;
+    case SO_BP1: str_tile<T, N, W, SO_BP1, Rs...>(d, tile, smem); return true;
+    case SO_BMID: str_tile<T, N, W, SO_BMID, Rs...>(d, tile, smem); return true;
+    case SO_COUT: str_tile<T, N, W, SO_COUT, Rs...>(d, tile, smem); return true;
+    default: return false;
+  }
+}
+
 // True when a pass's fused operations are one of the strided kernel's sets.
 __host__ __device__ inline bool str_ops_supported(uint32_t flags) {
   switch (flags & kStrOpMask) {
