@@ -89,3 +89,29 @@ def test_ragged_config4_full_size(gbfft_lib):
     rng = np.random.default_rng(4)
     sample = rng.choice(len(lengths), 300, replace=False)
     check_segments(lengths, modes, plan.offsets, x.numpy(), yn, sample=sample)
+
+
+def test_ragged_edge_cases(gbfft_lib):
+    """Zero-length and length-1 transforms inside a batch, a batch of only
+    length-1 transforms, and an empty batch."""
+    g = gbfft_lib
+    rng = np.random.default_rng(21)
+    lengths = np.array([0, 1, 0, 7, 1, 0, 4099, 2, 0], np.int64)
+    modes = np.array([-1, 1, 2, 2, -1, 1, 1, -1, 2], np.int32)
+    total = int(lengths.sum())
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    plan = g.RaggedPlan(lengths, modes)
+    y = plan(torch.from_numpy(x).cuda())
+    torch.cuda.synchronize()
+    assert plan.status() == 0
+    check_segments(lengths, modes, plan.offsets, x, y.cpu().numpy())
+    plan.close()
+    ones = np.ones(50, np.int64)
+    plan = g.RaggedPlan(ones, np.array([-1, 1] * 25, np.int32))
+    x1 = torch.from_numpy((rng.standard_normal(50) + 1j * rng.standard_normal(50)).astype(np.complex64)).cuda()
+    y1 = plan(x1)
+    torch.cuda.synchronize()
+    assert torch.equal(y1, x1)  # the DFT of length 1 is the identity in every mode
+    plan.close()
+    plan = g.RaggedPlan(np.zeros(0, np.int64), np.zeros(0, np.int32))
+    plan.close()
