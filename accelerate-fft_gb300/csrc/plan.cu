@@ -740,8 +740,10 @@ int create_plan(gbfft_plan** out, int rank, const int64_t* dims, int kind, int d
                 const TuneChoice* forced) {
   if (!out) return GBFFT_ERR_INVALID_ARG;
   *out = nullptr;
-  if (rank < 1 || rank > 3 || !dims) return GBFFT_ERR_INVALID_ARG;
+  if (rank < 1 || rank > 5 || !dims) return GBFFT_ERR_INVALID_ARG;
   if (kind != GBFFT_KIND_MANY && kind != GBFFT_KIND_FULL) return GBFFT_ERR_INVALID_ARG;
+  // rank 4-5: the innermost-axis transform only (as FFT.hs:63-84); no full 4D/5D
+  if (kind == GBFFT_KIND_FULL && rank > 3) return GBFFT_ERR_UNSUPPORTED;
   if (dtype != GBFFT_C32 && dtype != GBFFT_C64) return GBFFT_ERR_INVALID_ARG;
   if (precision != GBFFT_PLAIN && precision != GBFFT_SPLIT_FP16) return GBFFT_ERR_INVALID_ARG;
   int64_t total = 1;
@@ -1020,7 +1022,7 @@ int gbfft_plan_create(gbfft_plan** out, int rank, const int64_t* dims, int kind,
 
 int gbfft_autotune(int rank, const int64_t* dims, int kind, int dtype, int precision, void* stream,
                    char* report, size_t cap) {
-  if (!dims || rank < 1 || rank > 3) return GBFFT_ERR_INVALID_ARG;
+  if (!dims || rank < 1 || rank > 5) return GBFFT_ERR_INVALID_ARG;
   gbfft::TuneChoice best;
   std::string rep;
   const int st = gbfft::autotune_plan(rank, dims, kind, dtype, precision, stream, best, &rep);
@@ -1030,8 +1032,9 @@ int gbfft_autotune(int rank, const int64_t* dims, int kind, int dtype, int preci
 
 int gbfft_plan_explain(int rank, const int64_t* dims, int kind, int dtype, int precision, char* buf,
                        size_t cap) {
-  if (!buf || cap == 0 || !dims || rank < 1 || rank > 3) return GBFFT_ERR_INVALID_ARG;
+  if (!buf || cap == 0 || !dims || rank < 1 || rank > 5) return GBFFT_ERR_INVALID_ARG;
   if (kind != GBFFT_KIND_MANY && kind != GBFFT_KIND_FULL) return GBFFT_ERR_INVALID_ARG;
+  if (kind == GBFFT_KIND_FULL && rank > 3) return GBFFT_ERR_UNSUPPORTED;
   if (dtype != GBFFT_C32 && dtype != GBFFT_C64) return GBFFT_ERR_INVALID_ARG;
   gbfft_plan p;
   p.rank = rank;
@@ -1078,7 +1081,7 @@ int gbfft_exec(const gbfft_plan* plan, int mode, const void* d_in, void* d_out, 
 
 // ---- plan cache -----------------------------------------------------------
 namespace {
-using CacheKey = std::tuple<uintptr_t, int, int64_t, int64_t, int64_t, int, int, int>;
+using CacheKey = std::tuple<uintptr_t, int, int64_t, int64_t, int64_t, int64_t, int64_t, int, int, int>;
 std::mutex g_cache_mu;
 std::map<CacheKey, gbfft_plan*>& cache() {
   static auto* m = new std::map<CacheKey, gbfft_plan*>();
@@ -1108,12 +1111,12 @@ uintptr_t current_context() {
 
 int gbfft_plan_get(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype,
                    int precision) {
-  if (!out || !dims || rank < 1 || rank > 3) return GBFFT_ERR_INVALID_ARG;
+  if (!out || !dims || rank < 1 || rank > 5) return GBFFT_ERR_INVALID_ARG;
   // make sure a context exists before keying on it
   cudaFree(nullptr);
-  int64_t d[3] = {0, 0, 0};
+  int64_t d[5] = {0, 0, 0, 0, 0};
   for (int i = 0; i < rank; ++i) d[i] = dims[i];
-  CacheKey key{current_context(), rank, d[0], d[1], d[2], kind, dtype, precision};
+  CacheKey key{current_context(), rank, d[0], d[1], d[2], d[3], d[4], kind, dtype, precision};
   std::lock_guard<std::mutex> lk(g_cache_mu);
   auto it = cache().find(key);
   if (it != cache().end()) {

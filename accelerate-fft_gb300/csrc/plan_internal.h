@@ -101,7 +101,7 @@ bool feature_disabled(const char* what);  // GBFFT_DISABLE=tma,row,cluster (A/B 
 // The plan object behind the opaque gbfft_plan handle.
 struct gbfft_plan {
   int rank = 0;
-  int64_t dims[3] = {0, 0, 0};
+  int64_t dims[5] = {0, 0, 0, 0, 0};  // outermost first; rank 4-5 for batched-innermost plans
   int kind = 0, dtype = 0, precision = 0;
   int device = 0;
   bool dbl = false;

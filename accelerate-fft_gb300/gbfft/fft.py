@@ -145,8 +145,8 @@ def fft(mode, arr, stream=None):
     """DFT along the innermost axis (FFT.hs:63-84); any rank >= 1."""
     if arr.dim() < 1:
         raise ValueError("fft: rank >= 1 required")
-    if arr.dim() > 3:
-        # rank 4+: the batched-innermost plan over the flattened outer axes
+    if arr.dim() > 5:
+        # rank 6+: the batched-innermost plan over the flattened outer axes
         flat = arr.contiguous().reshape(-1, arr.shape[-1])
         return _run(L.KIND_MANY, mode, flat, stream).reshape(arr.shape)
     return _run(L.KIND_MANY, mode, arr, stream)

@@ -81,7 +81,9 @@ fft mode shR eR
   | Just Refl <- matchShapeR shR dim1 = fft1D mode eR
   | Just Refl <- matchShapeR shR dim2 = ForeignAcc "gbfft.fft2.many" $ fft' kindMany mode shR eR
   | Just Refl <- matchShapeR shR dim3 = ForeignAcc "gbfft.fft3.many" $ fft' kindMany mode shR eR
-  | otherwise = internalError "only for 1D..3D inner-dimension transforms"
+  -- ranks 4 and 5 (the reference falls back to its pure transform, FFT.hs:78)
+  | rank shR <= 5 = ForeignAcc ("gbfft.fft" ++ show (rank shR) ++ ".many") $ fft' kindMany mode shR eR
+  | otherwise = internalError "only for 1D..5D inner-dimension transforms"
 
 fft1D :: Mode -> NumericR e -> ForeignAcc (Array DIM1 (Vec2 e) -> Array DIM1 (Vec2 e))
 fft1D mode eR = ForeignAcc "gbfft.fft1d" $ fft' kindFull mode dim1 eR

@@ -50,9 +50,11 @@ enum { GBFFT_FORWARD = -1, GBFFT_REVERSE = 1, GBFFT_INVERSE = 2 };
 enum { GBFFT_C32 = 0 /* Complex Float, C2C */, GBFFT_C64 = 1 /* Complex Double, Z2Z */ };
 
 /* ---- transform kind ----------------------------------------------------
- * MANY: batched 1D transforms along the innermost axis of a rank-1..3
+ * MANY: batched 1D transforms along the innermost axis of a rank-1..5
  *       array -- PTX.fft (PTX.hs:52-61): "cuda.fft2.many" / "cuda.fft3.many"
- *       (cufftPlanMany [w] batch h or d*h, PTX.hs:158-170).
+ *       (cufftPlanMany [w] batch h or d*h, PTX.hs:158-170).  Ranks 4 and 5,
+ *       which the reference sends to its pure transform (FFT.hs:78), run on
+ *       the GPU here.
  * FULL: the rank-r transform over every axis -- PTX.fft1D/fft2D/fft3D
  *       (PTX.hs:63-70; cufftPlan1d/2d/3d, PTX.hs:137-156). */
 enum { GBFFT_KIND_MANY = 0, GBFFT_KIND_FULL = 1 };
@@ -72,8 +74,8 @@ int gbfft_version(void);
  * constructors the reference caches (PTX.hs:137-170).  Allocates the plan's
  * device workspace (twiddle tables, Bluestein chirp and filter spectrum,
  * scratch for multi-pass transforms) and synchronises the device once.
- * rank 1..3; dims outermost-first; a zero extent gives a plan whose exec is
- * a no-op. */
+ * rank 1..3 (1..5 for MANY); dims outermost-first; a zero extent gives a
+ * plan whose exec is a no-op. */
 int gbfft_plan_create(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype,
                       int precision);
 

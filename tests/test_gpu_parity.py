@@ -13,6 +13,8 @@ Tolerances (relative L2):
   plus the tolerance above (the reference's Float Bluestein forms its chirp
   angle in single precision, Adhoc.hs:264-265, so it is itself ~1e-4 off).
 """
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -451,3 +453,22 @@ def test_strided_input_not_16_byte_aligned(gbfft_lib, shape, kind):
     xv = view.cpu().numpy().astype(np.complex128)
     ref = np.fft.fft2(xv) if kind == "full" else np.fft.fft(xv, axis=-1)
     assert rel_l2(out.cpu().numpy(), ref) < 2e-6
+
+
+@pytest.mark.parametrize("shape", [(2, 3, 4, 5, 96), (3, 2, 2, 1009), (2, 2, 3, 4096)])
+def test_fft_rank4_and_5(gbfft_lib, shape):
+    """The innermost-axis transform of rank-4 and rank-5 arrays runs on the
+    GPU (the reference's PTX path stops at rank 3), in every mode."""
+    g = gbfft_lib
+    from gbfft import _lib as L
+    rng = np.random.default_rng(40)
+    x = uniform_complex(rng, shape, np.complex64)
+    for mode in MODES:
+        check(g, "fft", mode, x, same_precision=False)
+    # the C ABI takes the rank directly; a full 4D transform is not offered
+    dims = (ctypes.c_int64 * len(shape))(*shape)
+    h = ctypes.c_void_p()
+    assert L.lib().gbfft_plan_create(ctypes.byref(h), len(shape), dims, L.KIND_MANY, L.C32, L.PLAIN) == L.OK
+    L.lib().gbfft_plan_destroy(h)
+    assert L.lib().gbfft_plan_create(ctypes.byref(h), len(shape), dims, L.KIND_FULL, L.C32,
+                                     L.PLAIN) == L.ERR_UNSUPPORTED
