@@ -46,6 +46,8 @@ SIGNATURES = {
     "gbfft_plan_describe": (_i, [_vp, ctypes.c_char_p, _sz]),
     "gbfft_plan_pass_kernel": (_i, [_vp, _i, ctypes.c_char_p, _sz]),
     "gbfft_autotune": (_i, [_i, _i64p, _i, _i, _i, _vp, ctypes.c_char_p, _sz]),
+    "gbfft_dftG": (_i, [_i, _i64p, _i, _vp, _vp, _vp, _vp]),
+    "gbfft_dftGS": (_i, [_i, _i64p, _i, _i64, _vp, _vp, _vp, _vp]),
     "gbfft_tune_load": (_i, [ctypes.c_char_p]),
     "gbfft_tune_clear": (_i, []),
     "gbfft_tune_count": (_i, []),

@@ -173,6 +173,49 @@ def fft3D(mode, arr, stream=None):
     return _run(L.KIND_FULL, mode, arr, stream)
 
 
+def roots_of_unity(shape, inverse=False, dtype=torch.complex64, device="cuda"):
+    """rootsOfUnity / inverseRootsOfUnity (Roots.hs:26-51): element (sh :. i)
+    = cos t :+ (-+ sin t), t = 2*pi*i/n, computed in the element precision."""
+    n = int(shape[-1])
+    real = torch.float64 if dtype == torch.complex128 else torch.float32
+    t = (2 * torch.tensor(torch.pi, dtype=real) * torch.arange(n, dtype=real)) / n
+    r = torch.complex(torch.cos(t), torch.sin(t) if inverse else -torch.sin(t))
+    return r.expand(tuple(int(s) for s in shape)).contiguous().to(device)
+
+
+def dftG(roots, arr, stream=None):
+    """Math.DFT.dftG (DFT.hs:68-92) on the GPU, summing over every element as
+    the reference does (for rank > 1 every output row holds the same values)."""
+    if roots.shape != arr.shape or roots.dtype != arr.dtype:
+        raise ValueError("dftG: roots and input must have the same shape and type")
+    x = arr.contiguous()
+    out = torch.empty_like(x)
+    L.check(L.lib().gbfft_dftG(x.dim(), _dims(x.shape), _dtype_code(x), ctypes.c_void_p(roots.contiguous().data_ptr()),
+                               ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()), _stream(stream)),
+            "gbfft_dftG")
+    return out
+
+
+def dftGS(k, roots, arr, stream=None):
+    """Math.DFT.dftGS (DFT.hs:95-111): bin k of dftG, a 0-d tensor."""
+    x = arr.contiguous()
+    out = torch.empty((), dtype=x.dtype, device=x.device)
+    L.check(L.lib().gbfft_dftGS(x.dim(), _dims(x.shape), _dtype_code(x), int(k),
+                                ctypes.c_void_p(roots.contiguous().data_ptr()), ctypes.c_void_p(x.data_ptr()),
+                                ctypes.c_void_p(out.data_ptr()), _stream(stream)), "gbfft_dftGS")
+    return out
+
+
+def dft(arr, stream=None):
+    """Math.DFT.dft (DFT.hs:37-41): dftG with rootsOfUnity."""
+    return dftG(roots_of_unity(arr.shape, False, arr.dtype, arr.device), arr, stream)
+
+
+def idft(arr, stream=None):
+    """Math.DFT.idft (DFT.hs:44-53): dftG with inverseRootsOfUnity, then / n."""
+    return dftG(roots_of_unity(arr.shape, True, arr.dtype, arr.device), arr, stream) / arr.shape[-1]
+
+
 def ragged_autotune(lengths, modes, offsets=None, dtype=torch.complex64, stream=None):
     """Times candidate ragged plans for these lengths and modes
     (gbfft_ragged_autotune) and caches the fastest; returns the report."""

@@ -155,6 +155,21 @@ int gbfft_tune_clear(void);
 /* Number of tuned choices held. */
 int gbfft_tune_count(void);
 
+/* ---- naive DFT with caller-supplied roots: DFT.hs:68-111 ---------------
+ * gbfft_dftG replaces Math.DFT.dftG (DFT.hs:68-92) for an array of rank
+ * 1..5 (dims outermost-first) and roots of the same shape (rootsOfUnity /
+ * inverseRootsOfUnity, Roots.hs:26-51, or any others): out(sh_o :. k) =
+ * sum over ALL elements (sh :. n) of in(sh :. n) * roots(sh :. (k*n) mod l),
+ * l = the innermost extent -- the reference folds over an extended axis of
+ * length shapeSize, so for rank > 1 every output row holds the same values.
+ * gbfft_dftGS replaces dftGS (DFT.hs:95-111): that single value for bin k,
+ * written to d_out[0].  O(size * l) work, no allocation, asynchronous on
+ * `stream`. */
+int gbfft_dftG(int rank, const int64_t* dims, int dtype, const void* d_roots, const void* d_in, void* d_out,
+               void* stream);
+int gbfft_dftGS(int rank, const int64_t* dims, int dtype, int64_t k, const void* d_roots, const void* d_in,
+                void* d_out, void* stream);
+
 /* ---- ragged batch: new beyond the reference API -------------------------
  * `count` independent 1D transforms of uneven lengths over one flat buffer,
  * executed by one persistent launch (the reference can only express this as

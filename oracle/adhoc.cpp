@@ -504,9 +504,66 @@ static void dft_naive(int sign, const Cx<T>* x, Cx<T>* y, int64_t rows, int64_t 
   }
 }
 
+// dftG as written (DFT.hs:68-92): the input is extended with one more axis of
+// length shapeSize(base) and folded along it, so every output element
+// (sh_o :. k) is the sum over ALL input elements i = (sh_i :. n_i) of
+// arr[i] * roots[sh_i :. (k*n_i) mod l] -- for rank > 1 each output row holds
+// the transform of the sum of the rows (each row with its own roots); for
+// rank 1 it is the ordinary DFT.  Summed left to right in element order.
+template <typename T>
+static void dft_g(const Cx<T>* roots, const Cx<T>* x, Cx<T>* y, int64_t rows, int64_t l, int threads) {
+  const int64_t N = rows * l;
+  std::vector<Cx<T>> s(static_cast<size_t>(l));
+#pragma omp parallel for schedule(static) num_threads(threads) if (threads > 1)
+  for (int64_t k = 0; k < l; ++k) {
+    Cx<T> acc{T(0), T(0)};
+    for (int64_t i = 0; i < N; ++i) {
+      const int64_t r = i / l, n = i - r * l;
+      acc = add(acc, mul(x[i], roots[r * l + (k * n) % l]));
+    }
+    s[size_t(k)] = acc;
+  }
+  for (int64_t r = 0; r < rows; ++r)
+    for (int64_t k = 0; k < l; ++k) y[r * l + k] = s[size_t(k)];
+}
+
+// dftGS (DFT.hs:95-111): the single value sum over all (sh :. n) of
+// arr[sh :. n] * roots[sh :. (k*n) mod l] (foldAll), k = indexHead ix.
+template <typename T>
+static Cx<T> dft_gs(int64_t k, const Cx<T>* roots, const Cx<T>* x, int64_t rows, int64_t l) {
+  Cx<T> acc{T(0), T(0)};
+  for (int64_t r = 0; r < rows; ++r)
+    for (int64_t n = 0; n < l; ++n) acc = add(acc, mul(x[r * l + n], roots[r * l + (k * n) % l]));
+  return acc;
+}
+
 }  // namespace oracle
 
 extern "C" {
+
+// dftG / dftGS over `rows` x `l` (rows = product of the outer extents).
+int oracle_dftg_f32(int64_t rows, int64_t l, const float* roots, const float* in, float* out, int threads) {
+  if (l <= 0 || rows < 0) return 1;
+  oracle::dft_g<float>(reinterpret_cast<const oracle::Cx<float>*>(roots),
+                       reinterpret_cast<const oracle::Cx<float>*>(in), reinterpret_cast<oracle::Cx<float>*>(out),
+                       rows, l, threads);
+  return 0;
+}
+int oracle_dftg_f64(int64_t rows, int64_t l, const double* roots, const double* in, double* out, int threads) {
+  if (l <= 0 || rows < 0) return 1;
+  oracle::dft_g<double>(reinterpret_cast<const oracle::Cx<double>*>(roots),
+                        reinterpret_cast<const oracle::Cx<double>*>(in),
+                        reinterpret_cast<oracle::Cx<double>*>(out), rows, l, threads);
+  return 0;
+}
+int oracle_dftgs_f64(int64_t k, int64_t rows, int64_t l, const double* roots, const double* in, double* out) {
+  if (l <= 0 || rows < 0 || k < 0) return 1;
+  const auto v = oracle::dft_gs<double>(k, reinterpret_cast<const oracle::Cx<double>*>(roots),
+                                        reinterpret_cast<const oracle::Cx<double>*>(in), rows, l);
+  out[0] = v.re;
+  out[1] = v.im;
+  return 0;
+}
 
 // Status: 0 ok, 1 bad argument.  Buffers hold interleaved (re, im) pairs.
 int oracle_fft_f32(int mode, int kind, int rank, const int64_t* dims, const float* in, float* out,

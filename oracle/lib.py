@@ -3,8 +3,9 @@
 Functions mirror accelerate-fft's API: ``fft`` (innermost axis, FFT.hs:63-84),
 ``fft1D`` / ``fft2D`` / ``fft3D`` (FFT.hs:92-173) with Mode Forward / Reverse /
 Inverse, in the precision of the input (complex64 -> Float, complex128 ->
-Double); plus ``dft_naive`` (DFT.hs:68-92 in FP64) and ``ceiling5_smooth``
-(Adhoc.hs:289-313).
+Double); plus ``dft_naive`` (an FP64 per-row DFT), ``dftG`` / ``dftGS`` and
+``roots_of_unity`` as the reference writes them (DFT.hs:68-111, Roots.hs:26-51)
+and ``ceiling5_smooth`` (Adhoc.hs:289-313).
 """
 import ctypes
 import os
@@ -34,6 +35,14 @@ def lib():
         _lib.oracle_dft_naive_f64.restype = ctypes.c_int
         _lib.oracle_ceiling5_smooth.argtypes = [ctypes.c_int64]
         _lib.oracle_ceiling5_smooth.restype = ctypes.c_int64
+        for name in ("oracle_dftg_f32", "oracle_dftg_f64"):
+            f = getattr(_lib, name)
+            f.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                          ctypes.c_int]
+            f.restype = ctypes.c_int
+        _lib.oracle_dftgs_f64.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p]
+        _lib.oracle_dftgs_f64.restype = ctypes.c_int
     return _lib
 
 
@@ -89,6 +98,46 @@ def dft_naive(sign, x, threads=None):
     if st != 0:
         raise ValueError("oracle: bad arguments for dft_naive")
     return out
+
+
+def roots_of_unity(shape, inverse=False, dtype=np.complex128):
+    """rootsOfUnity / inverseRootsOfUnity (Roots.hs:26-51): element
+    (sh :. i) = cos t :+ (-+ sin t), t = 2*pi*i/n, in the element precision."""
+    n = shape[-1]
+    real = np.float32 if dtype == np.complex64 else np.float64
+    t = (real(2) * real(np.pi) * np.arange(n, dtype=real)) / real(n)
+    r = (np.cos(t) + (1j if inverse else -1j) * np.sin(t)).astype(dtype)
+    return np.ascontiguousarray(np.broadcast_to(r, shape))
+
+
+def dftG(roots, x, threads=None):
+    """dftG as written (DFT.hs:68-92): every output row is the sum over all
+    input elements (sh :. n) of x * roots[sh :. (k*n) mod l]."""
+    x = np.ascontiguousarray(x)
+    roots = np.ascontiguousarray(roots, dtype=x.dtype)
+    if roots.shape != x.shape:
+        raise ValueError("oracle: roots and input shapes differ")
+    f = lib().oracle_dftg_f32 if x.dtype == np.complex64 else lib().oracle_dftg_f64
+    l = x.shape[-1]
+    rows = x.size // max(l, 1)
+    out = np.empty_like(x)
+    if threads is None:
+        threads = os.cpu_count() or 1
+    if f(rows, l, roots.ctypes.data, x.ctypes.data, out.ctypes.data, int(threads)) != 0:
+        raise ValueError("oracle: bad arguments for dftG")
+    return out
+
+
+def dftGS(k, roots, x):
+    """dftGS (DFT.hs:95-111) in FP64: one bin, summed over every row."""
+    x = np.ascontiguousarray(x, dtype=np.complex128)
+    roots = np.ascontiguousarray(roots, dtype=np.complex128)
+    l = x.shape[-1]
+    rows = x.size // max(l, 1)
+    out = np.empty(1, np.complex128)
+    if lib().oracle_dftgs_f64(int(k), rows, l, roots.ctypes.data, x.ctypes.data, out.ctypes.data) != 0:
+        raise ValueError("oracle: bad arguments for dftGS")
+    return out[0]
 
 
 def ceiling5_smooth(n):

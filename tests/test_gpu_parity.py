@@ -241,7 +241,9 @@ def test_error_codes(gbfft_lib):
     h = ctypes.c_void_p()
     dims = (ctypes.c_int64 * 2)(4, 4)
     assert lib.gbfft_plan_create(ctypes.byref(h), 0, dims, 1, 0, 0) == L.ERR_INVALID_ARG
-    assert lib.gbfft_plan_create(ctypes.byref(h), 4, dims, 1, 0, 0) == L.ERR_INVALID_ARG
+    assert lib.gbfft_plan_create(ctypes.byref(h), 6, dims, 0, 0, 0) == L.ERR_INVALID_ARG
+    dims4 = (ctypes.c_int64 * 4)(2, 2, 4, 4)
+    assert lib.gbfft_plan_create(ctypes.byref(h), 4, dims4, 1, 0, 0) == L.ERR_UNSUPPORTED  # no full 4D
     assert lib.gbfft_plan_create(ctypes.byref(h), 2, dims, 7, 0, 0) == L.ERR_INVALID_ARG
     assert lib.gbfft_plan_create(ctypes.byref(h), 2, dims, 1, 3, 0) == L.ERR_INVALID_ARG
     neg = (ctypes.c_int64 * 2)(4, -1)
