@@ -209,7 +209,7 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(64 * W / U, MINB)
       if (fl & F_SCALE) e = cscale(e, s);
       if (fl & F_CONJ_OUT) e.y = -e.y;
       const int row = K + 64 * (kb1 + 8 * kb2);
-      out[int64_t(row) * oes + x] = e;
+      out[int64_t(row) * oes + x + rot_delta(d, row)] = e;
     }
   }
 }
@@ -350,7 +350,7 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(64 * W / U, MINB)
       C e = v[u][kb2];
       if (fl & F_SCALE) e = cscale(e, s);
       if (fl & F_CONJ_OUT) e.y = -e.y;
-      out[int64_t(K + 64 * (kb1 + 8 * kb2)) * oes + x] = e;
+      out[int64_t(K + 64 * (kb1 + 8 * kb2)) * oes + x + rot_delta(d, K + 64 * (kb1 + 8 * kb2))] = e;
     }
   }
 }
@@ -489,7 +489,7 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
     C e = v[lambda];
     if (fl & F_SCALE) e = cscale(e, s);
     if (fl & F_CONJ_OUT) e.y = -e.y;
-    out[int64_t(K1 + 16 * kappa + 256 * lambda) * oes + x] = e;
+    out[int64_t(K1 + 16 * kappa + 256 * lambda) * oes + x + rot_delta(d, K1 + 16 * kappa + 256 * lambda)] = e;
   }
 }
 
@@ -603,7 +603,7 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
       C e = v[lambda];
       if (fl & F_SCALE) e = cscale(e, s);
       if (fl & F_CONJ_OUT) e.y = -e.y;
-      out[int64_t(K1 + 16 * kappa + 256 * lambda) * oes + x] = e;
+      out[int64_t(K1 + 16 * kappa + 256 * lambda) * oes + x + rot_delta(d, K1 + 16 * kappa + 256 * lambda)] = e;
     }
   }
   // a timed-out wait may leave a copy landing in this CTA's buffers: wait

@@ -1,6 +1,7 @@
 // Naive DFT with caller-supplied roots of unity, as the reference defines it
 // (Data.Array.Accelerate.Math.DFT, DFT.hs:68-111) -- for single bins and tiny
-// lengths, where a transform plan does not pay off.
+// lengths, where a transform plan does not pay off -- and the centring and
+// shifting helpers of Math.DFT.Centre.
 //
 // dftG roots arr: the reference extends the input with one more axis of
 // length shapeSize(arr) and folds along it, so every output element
@@ -93,6 +94,61 @@ __global__ void __launch_bounds__(kDftThreads) dftgs_kernel(int64_t k, const typ
   if (threadIdx.x == 0) out[0] = s;
 }
 
+// Centre.hs (DFT/Centre.hs:36-164) for rank 1..3, dims outermost-first:
+//   centre: out(z, y, x) = (-1)^(z + y + x) * in(z, y, x)
+//   shift:  out(z, y, x) = in((z + sd) mod d, (y + sh) mod h, (x + sw) mod w)
+// with s = n/2 + (n odd) for shift, n/2 for ishift, per axis.  One pass,
+// grid-stride over the output, the multi-index from two divisions.
+struct Dims3 {
+  int64_t d, h, w;
+  int64_t sd, sh, sw;
+};
+
+template <typename C>
+__global__ void centre_kernel(const C* __restrict__ in, C* __restrict__ out, Dims3 g) {
+  const int64_t total = g.d * g.h * g.w;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t x = i % g.w, yz = i / g.w, y = yz % g.h, z = yz / g.h;
+    C v = in[i];
+    if ((x + y + z) & 1) {
+      v.x = -v.x;
+      v.y = -v.y;
+    }
+    out[i] = v;
+  }
+}
+
+template <typename C>
+__global__ void shift_kernel(const C* __restrict__ in, C* __restrict__ out, Dims3 g) {
+  const int64_t total = g.d * g.h * g.w;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t x = i % g.w, yz = i / g.w, y = yz % g.h, z = yz / g.h;
+    int64_t xs = x + g.sw, ys = y + g.sh, zs = z + g.sd;
+    if (xs >= g.w) xs -= g.w;
+    if (ys >= g.h) ys -= g.h;
+    if (zs >= g.d) zs -= g.d;
+    out[i] = in[(zs * g.h + ys) * g.w + xs];
+  }
+}
+
+int dims3(int rank, const int64_t* dims, Dims3& g) {
+  if (rank < 1 || rank > 3 || !dims) return GBFFT_ERR_INVALID_ARG;
+  int64_t e[3] = {1, 1, 1};
+  for (int i = 0; i < rank; ++i) {
+    if (dims[i] < 0) return GBFFT_ERR_INVALID_ARG;
+    e[3 - rank + i] = dims[i];
+  }
+  g.d = e[0];
+  g.h = e[1];
+  g.w = e[2];
+  return GBFFT_OK;
+}
+
+unsigned grid_for(int64_t total) {
+  const int64_t b = (total + 255) / 256;
+  return unsigned(b < 8192 ? (b > 0 ? b : 1) : 8192);
+}
+
 int shape_rows(int rank, const int64_t* dims, int64_t& rows, int64_t& l) {
   if (rank < 1 || rank > 5 || !dims) return GBFFT_ERR_INVALID_ARG;
   rows = 1;
@@ -159,6 +215,47 @@ int gbfft_dftGS(int rank, const int64_t* dims, int dtype, int64_t k, const void*
     dftgs_kernel<float><<<1, kDftThreads, 0, s>>>(k, static_cast<const float2*>(d_roots),
                                                   static_cast<const float2*>(d_in), static_cast<float2*>(d_out),
                                                   rows, l);
+  return cudaGetLastError() == cudaSuccess ? GBFFT_OK : GBFFT_ERR_CUDA;
+}
+
+int gbfft_centre(int rank, const int64_t* dims, int dtype, const void* d_in, void* d_out, void* stream) {
+  Dims3 g{};
+  int st = dims3(rank, dims, g);
+  if (st != GBFFT_OK) return st;
+  if (dtype != GBFFT_C32 && dtype != GBFFT_C64) return GBFFT_ERR_INVALID_ARG;
+  const int64_t total = g.d * g.h * g.w;
+  if (total == 0) return GBFFT_OK;
+  if (!d_in || !d_out) return GBFFT_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (dtype == GBFFT_C64)
+    centre_kernel<double2><<<grid_for(total), 256, 0, s>>>(static_cast<const double2*>(d_in),
+                                                          static_cast<double2*>(d_out), g);
+  else
+    centre_kernel<float2><<<grid_for(total), 256, 0, s>>>(static_cast<const float2*>(d_in),
+                                                         static_cast<float2*>(d_out), g);
+  return cudaGetLastError() == cudaSuccess ? GBFFT_OK : GBFFT_ERR_CUDA;
+}
+
+int gbfft_shift(int rank, const int64_t* dims, int dtype, int inverse, const void* d_in, void* d_out,
+                void* stream) {
+  Dims3 g{};
+  int st = dims3(rank, dims, g);
+  if (st != GBFFT_OK) return st;
+  if (dtype != GBFFT_C32 && dtype != GBFFT_C64) return GBFFT_ERR_INVALID_ARG;
+  const int64_t total = g.d * g.h * g.w;
+  if (total == 0) return GBFFT_OK;
+  if (!d_in || !d_out || d_in == d_out) return GBFFT_ERR_INVALID_ARG;
+  auto sft = [&](int64_t n) { return n / 2 + (inverse ? 0 : (n & 1)); };
+  g.sd = sft(g.d);
+  g.sh = sft(g.h);
+  g.sw = sft(g.w);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (dtype == GBFFT_C64)
+    shift_kernel<double2><<<grid_for(total), 256, 0, s>>>(static_cast<const double2*>(d_in),
+                                                         static_cast<double2*>(d_out), g);
+  else
+    shift_kernel<float2><<<grid_for(total), 256, 0, s>>>(static_cast<const float2*>(d_in),
+                                                        static_cast<float2*>(d_out), g);
   return cudaGetLastError() == cudaSuccess ? GBFFT_OK : GBFFT_ERR_CUDA;
 }
 

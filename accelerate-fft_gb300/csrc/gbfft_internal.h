@@ -37,6 +37,7 @@ enum PassFlags : uint32_t {
   F_SPEC = 1u << 11,       // in-kernel spectral multiply: DFT, * filter[l], conj, DFT
   F_L2_IN_FIRST = 1u << 12,  // loads: L2 evict_first (input read once)
   F_L2_OUT_LAST = 1u << 13,  // stores: L2 evict_last (a later pass reads them back)
+  F_ROT_OUT = 1u << 14,      // stores: output index l along the axis goes to (l - rot_s) mod rot_n
 };
 
 // Kernel families a pass can run on.
@@ -96,12 +97,21 @@ struct PassDesc {
   const int64_t* col_out_off;
   const void* chirp;   // Bluestein chirp c[l] = exp(-i*pi*l^2/n), l < n
   const void* filter;  // Bluestein filter spectrum DFT(conj chirp)/m, length m
+  // F_ROT_OUT (shift / ishift fused into the last pass of an axis): the
+  // element with axis index l = k*lout_es + c*lout_cs is stored
+  // (rot(l) - l) * rot_stride elements away, rot(l) = (l - rot_s) mod rot_n
+  int64_t rot_n, rot_s, rot_stride;
 };
+
+// Address offset of F_ROT_OUT for axis index l (0 without the flag).
+__host__ __device__ inline int64_t rot_delta(const PassDesc& d, int64_t l) {
+  if (!(d.flags & F_ROT_OUT)) return 0;
+  return (l >= d.rot_s ? -d.rot_s : d.rot_n - d.rot_s) * d.rot_stride;
+}
 
 size_t pass_smem_bytes(const PassDesc& d, bool is_double);
 int pass_grid(const PassDesc& d);
 
-// Launch one pencil pass on `stream`; returns a cudaError_t.
 // cuTensorMapEncodeTiled from the driver (nullptr when unavailable).
 void* tensor_map_encode_fn();
 
@@ -109,6 +119,7 @@ void* tensor_map_encode_fn();
 // input assumed).
 const char* pass_kernel_name(const PassDesc& d, bool is_double);
 const char* str_kernel_name(const PassDesc& d, bool is_double);
+// Launch one pass on `stream`; returns a cudaError_t.
 cudaError_t launch_pass(const PassDesc& d, bool is_double, cudaStream_t stream);
 
 // Prepare kernel attributes (max dynamic shared memory); idempotent.

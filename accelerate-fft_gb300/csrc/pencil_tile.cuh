@@ -182,7 +182,7 @@ __device__ __forceinline__ void pencil_store(const PassDesc& d, typename CxT<T>:
   const C* __restrict__ chirp = static_cast<const C*>(d.chirp);
   const int64_t tw4_mask = (int64_t(1) << d.tw4_shift) - 1;
   const T sc = (fl & F_SCALE) ? T(d.scale) : T(1);
-  const bool need_l = (fl & (F_FILTER_OUT | F_CHIRP_OUT | F_BLUE | F_TRUNC_OUT)) != 0;
+  const bool need_l = (fl & (F_FILTER_OUT | F_CHIRP_OUT | F_BLUE | F_TRUNC_OUT | F_ROT_OUT)) != 0;
   const I oes = I(d.out_es), ocs = I(d.out_cs);
   C* __restrict__ base = out + (d.col_out_off ? 0 : c0 * d.out_cs);
   for (int f0 = threadIdx.x; f0 < total; f0 += KU * step) {
@@ -246,7 +246,7 @@ __device__ __forceinline__ void pencil_store(const PassDesc& d, typename CxT<T>:
       C e = v[u];
       if (fl & F_SCALE) e = cscale(e, sc);
       if (fl & F_CONJ_OUT) e.y = -e.y;
-      base[cofs[u] + ofs[u]] = e;
+      base[cofs[u] + ofs[u] + rot_delta(d, lidx[u])] = e;
     }
   }
 }

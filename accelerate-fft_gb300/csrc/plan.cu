@@ -480,6 +480,11 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     }
     ps.src = src;
     ps.dst = R_OUT;
+    ps.d.lout_es = 1;  // axis index = element index k
+    ps.d.lout_cs = 0;
+    ps.axis_final = ps.rot_ok = true;
+    ps.axis_n = ax.n;
+    ps.rot_stride = ax.es;
     passes.push_back(ps);
     std::snprintf(buf, sizeof buf, "[n=%lld r=%s es=%lld %s W=%d]", (long long)ax.n, radix_list(ps.d).c_str(),
                   (long long)ax.es, kname, ps.d.W);
@@ -545,6 +550,15 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     p1.dst = mid;
     p2.src = mid;
     p2.dst = R_OUT;
+    p2.axis_final = true;
+    p2.axis_n = ax.n;
+    if (ax.es == 1) {
+      // rows: output k = k1 + n1*k2, k2 the element index, k1 the column
+      p2.d.lout_es = n1;
+      p2.d.lout_cs = 1;
+      p2.rot_ok = true;
+      p2.rot_stride = 1;
+    }
     passes.push_back(p1);
     passes.push_back(p2);
     std::snprintf(buf, sizeof buf, "[n=%lld=%lldx%lld four-step es=%lld W=%d,%d]", (long long)ax.n,
@@ -586,6 +600,9 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     if (rowk) d.kernel = K_ROW;  // register-resident rows
     ps.src = src;
     ps.dst = R_OUT;
+    ps.axis_final = ps.rot_ok = true;  // axis index = k (lout_es 1, lout_cs 0)
+    ps.axis_n = ax.n;
+    ps.rot_stride = ax.es;
     passes.push_back(ps);
     std::snprintf(buf, sizeof buf, "[n=%lld bluestein m=%lld es=%lld %s W=%d]", (long long)ax.n,
                   (long long)m, (long long)ax.es, rowk ? "row" : "pencil", ps.d.W);
@@ -706,6 +723,9 @@ int add_bluestein_multipass(Builder& B, std::vector<PassSpec>& passes, const Axi
   p[1].dst = R_S2;
   p[2].src = R_S2;
   p[2].dst = R_OUT;
+  p[2].axis_final = p[2].rot_ok = true;  // axis index j1*m2 + j2 (lout_es m2, lout_cs 1)
+  p[2].axis_n = ax.n;
+  p[2].rot_stride = 1;
   for (int i = 0; i < 3; ++i) {
     choose_tile(p[i], dbl);
     use_strided(p[i], dbl);
@@ -964,8 +984,18 @@ class ScratchOrder {
   std::unique_lock<std::mutex> lk_;
 };
 
+// rotation of an axis of length n for the output options (shift, ishift,
+// centring of even lengths by the shift theorem)
+static int64_t axis_rotation(int64_t n, int opts, bool centre_fused) {
+  int64_t s = 0;
+  if (opts & GBFFT_OPT_SHIFT_OUT) s += n / 2 + (n & 1);
+  if (opts & GBFFT_OPT_ISHIFT_OUT) s += n / 2;
+  if (centre_fused) s += n / 2;
+  return n > 0 ? s % n : 0;
+}
+
 int exec_passes(const gbfft_plan* p, const std::vector<PassSpec>& passes, int mode, double inv_norm,
-                const void* in, void* out, cudaStream_t s) {
+                const void* in, void* out, cudaStream_t s, int opts, bool centre_fused) {
   const ScratchOrder order(p, s);
   if (passes.empty()) {
     // every axis has length <= 1: the DFT is the identity
@@ -986,6 +1016,15 @@ int exec_passes(const gbfft_plan* p, const std::vector<PassSpec>& passes, int mo
     if (mode == GBFFT_INVERSE && i == last) {
       d.flags |= F_SCALE;
       d.scale = inv_norm;
+    }
+    if (passes[i].axis_final && (opts || centre_fused)) {
+      const int64_t rot = axis_rotation(passes[i].axis_n, opts, centre_fused);
+      if (rot) {
+        d.flags |= F_ROT_OUT;
+        d.rot_n = passes[i].axis_n;
+        d.rot_s = rot;
+        d.rot_stride = passes[i].rot_stride;
+      }
     }
     if (launch_pass(d, p->dbl, s) != cudaSuccess) return GBFFT_ERR_CUDA;
   }
@@ -1077,6 +1116,78 @@ int gbfft_exec(const gbfft_plan* plan, int mode, const void* d_in, void* d_out, 
     return GBFFT_ERR_INVALID_ARG;
   return exec_passes(plan, plan->passes, mode, plan->inv_norm, d_in, d_out,
                      static_cast<cudaStream_t>(stream));
+}
+
+int gbfft_exec_ex(const gbfft_plan* plan, int mode, const void* d_in, void* d_out, void* stream, int opts) {
+  if (!opts) return gbfft_exec(plan, mode, d_in, d_out, stream);
+  if (!plan) return GBFFT_ERR_NULL_PLAN;
+  if (mode != GBFFT_FORWARD && mode != GBFFT_REVERSE && mode != GBFFT_INVERSE) return GBFFT_ERR_INVALID_ARG;
+  const int known = GBFFT_OPT_SHIFT_OUT | GBFFT_OPT_ISHIFT_OUT | GBFFT_OPT_CENTRE_IN;
+  if ((opts & ~known) || ((opts & GBFFT_OPT_SHIFT_OUT) && (opts & GBFFT_OPT_ISHIFT_OUT))) return GBFFT_ERR_INVALID_ARG;
+  // centre / shift are defined on the whole array (Centre.hs: 1D..3D)
+  if (plan->kind != GBFFT_KIND_FULL || plan->rank > 3) return GBFFT_ERR_INVALID_ARG;
+  if (plan->total == 0) return GBFFT_OK;
+  if (!d_in || !d_out || d_in == d_out) return GBFFT_ERR_INVALID_ARG;
+  const uintptr_t align = plan->dbl ? 16 : 8;
+  if ((reinterpret_cast<uintptr_t>(d_in) | reinterpret_cast<uintptr_t>(d_out)) & (align - 1))
+    return GBFFT_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  bool all_even = true;
+  for (int i = 0; i < plan->rank; ++i) all_even = all_even && (plan->dims[i] % 2 == 0);
+  const bool centre = (opts & GBFFT_OPT_CENTRE_IN) != 0;
+  const bool centre_fused = centre && all_even;  // centring = shifting the output by n/2
+  const int out_opts = opts & (GBFFT_OPT_SHIFT_OUT | GBFFT_OPT_ISHIFT_OUT);
+  // fused only when every axis of length > 1 ends in exactly one pass that
+  // can rotate its store index (the split-FP16 passes mark none)
+  int finals = 0, axes = 0;
+  bool fuse = true;
+  for (int i = 0; i < plan->rank; ++i) axes += plan->dims[i] > 1;
+  for (const PassSpec& ps : plan->passes) {
+    if (!ps.axis_final) continue;
+    ++finals;
+    if (axis_rotation(ps.axis_n, out_opts, centre_fused) && !ps.rot_ok) fuse = false;
+  }
+  if (finals != axes) fuse = false;
+  const size_t bytes = size_t(plan->total) * (plan->dbl ? 16 : 8);
+  const int dtype = plan->dbl ? GBFFT_C64 : GBFFT_C32;
+  const void* src = d_in;
+  void* tmp_in = nullptr;
+  void* tmp_out = nullptr;
+  int st = GBFFT_OK;
+  if (centre && !centre_fused) {
+    // odd lengths: the sign pattern is not a rotation; one pass before
+    if (cudaMallocAsync(&tmp_in, bytes, s) != cudaSuccess) return GBFFT_ERR_ALLOC;
+    st = gbfft_centre(plan->rank, plan->dims, dtype, d_in, tmp_in, stream);
+    src = tmp_in;
+  }
+  if (st == GBFFT_OK) {
+    if (fuse) {
+      st = exec_passes(plan, plan->passes, mode, plan->inv_norm, src, d_out, s, out_opts, centre_fused);
+    } else {
+      // an axis whose last pass cannot rotate: transform, then one shift pass
+      if (cudaMallocAsync(&tmp_out, bytes, s) != cudaSuccess) {
+        st = GBFFT_ERR_ALLOC;
+      } else {
+        st = exec_passes(plan, plan->passes, mode, plan->inv_norm, src, tmp_out, s);
+        if (st == GBFFT_OK && centre_fused)
+          st = gbfft_shift(plan->rank, plan->dims, dtype, 1, tmp_out, d_out, stream);  // n/2 = ishift for even n
+        if (st == GBFFT_OK && out_opts) {
+          const void* from = centre_fused ? d_out : tmp_out;
+          void* to = centre_fused ? tmp_out : d_out;
+          st = gbfft_shift(plan->rank, plan->dims, dtype, (out_opts & GBFFT_OPT_ISHIFT_OUT) ? 1 : 0, from, to, stream);
+          if (st == GBFFT_OK && centre_fused &&
+              cudaMemcpyAsync(d_out, tmp_out, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            st = GBFFT_ERR_CUDA;
+        } else if (st == GBFFT_OK && !centre_fused &&
+                   cudaMemcpyAsync(d_out, tmp_out, bytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+          st = GBFFT_ERR_CUDA;
+        }
+      }
+    }
+  }
+  if (tmp_in) cudaFreeAsync(tmp_in, s);
+  if (tmp_out) cudaFreeAsync(tmp_out, s);
+  return st;
 }
 
 // ---- plan cache -----------------------------------------------------------

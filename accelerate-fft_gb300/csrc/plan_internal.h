@@ -22,6 +22,11 @@ enum Role { R_IN = 0, R_OUT = 1, R_S1 = 2, R_S2 = 3 };
 struct PassSpec {
   PassDesc d;
   int src = R_IN, dst = R_OUT;
+  // the last pass of an axis: a fused output shift rotates axis index
+  // l = k*lout_es + c*lout_cs, stored rot_stride elements apart; rot_ok is
+  // false where the axis index is not of that form (strided four-step)
+  bool axis_final = false, rot_ok = false;
+  int64_t axis_n = 0, rot_stride = 0;
   // byte offsets into the plan's table blob (-1: none)
   int64_t tw_off = -1, tw4lo_off = -1, tw4hi_off = -1, chirp_off = -1, filter_off = -1;
 };
@@ -156,5 +161,5 @@ int create_plan(gbfft_plan** out, int rank, const int64_t* dims, int kind, int d
                 const TuneChoice* forced);
 int build_split_plan(gbfft_plan* p);
 int exec_passes(const gbfft_plan* p, const std::vector<PassSpec>& passes, int mode, double inv_norm,
-                const void* in, void* out, cudaStream_t s);
+                const void* in, void* out, cudaStream_t s, int opts = 0, bool centre_fused = false);
 }  // namespace gbfft

@@ -102,7 +102,8 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_kernel(const PassDe
       C x = v[q * RZ + r];
       if (fl & F_SCALE) x = cscale(x, s);
       if (fl & F_CONJ_OUT) x.y = -x.y;
-      out[t + TH * (q + r * (E / RZ))] = x;
+      const int k = t + TH * (q + r * (E / RZ));
+      out[k + rot_delta(d, k)] = x;
     }
 }
 
@@ -150,7 +151,8 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft1_kernel(const PassD
       C x = v[q * RZ + r];
       if (fl & F_SCALE) x = cscale(x, s);
       if (fl & F_CONJ_OUT) x.y = -x.y;
-      C* o = out + t + TH * (q + r * (E / RZ));
+      const int k = t + TH * (q + r * (E / RZ));
+      C* o = out + k + rot_delta(d, k);
       if (keep)
         st_l2hint(o, x, pol);
       else
@@ -226,7 +228,7 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowblue_kernel(const PassD
       C x = cmul(cconj(v[q * RZ + r]), chirp[k]);
       if (fl & F_SCALE) x = cscale(x, s);
       if (fl & F_CONJ_OUT) x.y = -x.y;
-      out[k] = x;
+      out[k + rot_delta(d, k)] = x;
     }
 }
 
@@ -308,7 +310,8 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_tma_kernel(const Pa
           C x = v[q * RZ + r];
           if (fl & F_SCALE) x = cscale(x, s);
           if (fl & F_CONJ_OUT) x.y = -x.y;
-          o[t + TH * (q + r * (E / RZ))] = x;
+          const int k = t + TH * (q + r * (E / RZ));
+          o[k + rot_delta(d, k)] = x;
         }
     }
   }
@@ -547,7 +550,8 @@ __global__ void __launch_bounds__(ROWS*(N / 16), MINB) rowfft_tc_kernel(const Pa
           C x = v[q * RZ + r];
           if (fl & F_SCALE) x = cscale(x, s);
           if (fl & F_CONJ_OUT) x.y = -x.y;
-          out[t + TH * (q + r * (E / RZ))] = x;
+          const int k = t + TH * (q + r * (E / RZ));
+          out[k + rot_delta(d, k)] = x;
         }
     }
     __syncthreads();  // the exchange buffer is reused by the next chunk

@@ -340,8 +340,9 @@ __device__ __forceinline__ void str_finish(const PassDesc& d, const StrCtx& c,
       for (int r = 0; r < RZ; ++r) {
         const int m = q + r * (E / RZ);
         C e = v[q * RZ + r];
-        if (!post(e, t + TH * m, col)) continue;
-        C* o = o0 + int64_t(TH * m) * oes;
+        const int k = t + TH * m;
+        if (!post(e, k, col)) continue;
+        C* o = o0 + int64_t(TH * m) * oes + rot_delta(d, int64_t(k) * d.lout_es + col * d.lout_cs);
         if (keep)
           st_l2hint(o, e, pol);
         else
@@ -370,7 +371,7 @@ __device__ __forceinline__ void str_finish(const PassDesc& d, const StrCtx& c,
       C e = b[k * W + (cc ^ (k & (W - 1)))];
       if (!post(e, k, cl)) continue;
       const int64_t cb = d.col_out_off ? d.col_out_off[cl] : cl * d.out_cs;
-      C* o = out + cb + int64_t(k) * oes;
+      C* o = out + cb + int64_t(k) * oes + rot_delta(d, int64_t(k) * d.lout_es + cl * d.lout_cs);
       if (keep)
         st_l2hint(o, e, pol);
       else

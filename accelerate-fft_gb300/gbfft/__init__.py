@@ -6,5 +6,5 @@ complex64 (Complex Float) and complex128 (Complex Double) CUDA tensors, all
 served by libgbfft.so through its C ABI (include/gbfft.h).
 """
 from ._lib import GbfftError, lib, error_string  # noqa: F401
-from .fft import (Mode, Plan, RaggedPlan, SpecConvPlan, autotune, dft, dftG, dftGS, fft,  # noqa: F401
-                  fft1D, fft2D, fft3D, idft, mode_code, ragged_autotune, roots_of_unity)
+from .fft import (Mode, Plan, RaggedPlan, SpecConvPlan, autotune, centre, dft, dftG, dftGS,  # noqa: F401
+                  fft, fft1D, fft2D, fft3D, idft, mode_code, ragged_autotune, roots_of_unity, shift)

@@ -23,6 +23,7 @@ FORWARD, REVERSE, INVERSE = -1, 1, 2
 C32, C64 = 0, 1
 KIND_MANY, KIND_FULL = 0, 1
 PLAIN, SPLIT_FP16 = 0, 1
+OPT_SHIFT_OUT, OPT_ISHIFT_OUT, OPT_CENTRE_IN = 1, 2, 4
 
 _vp = ctypes.c_void_p
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -37,6 +38,7 @@ SIGNATURES = {
     "gbfft_plan_create": (_i, [ctypes.POINTER(_vp), _i, _i64p, _i, _i, _i]),
     "gbfft_plan_destroy": (_i, [_vp]),
     "gbfft_exec": (_i, [_vp, _i, _vp, _vp, _vp]),
+    "gbfft_exec_ex": (_i, [_vp, _i, _vp, _vp, _vp, _i]),
     "gbfft_plan_get": (_i, [ctypes.POINTER(_vp), _i, _i64p, _i, _i, _i]),
     "gbfft_fft": (_i, [_i, _i, _i64p, _i, _i, _vp, _vp, _vp]),
     "gbfft_cache_clear": (_i, []),
@@ -48,6 +50,8 @@ SIGNATURES = {
     "gbfft_autotune": (_i, [_i, _i64p, _i, _i, _i, _vp, ctypes.c_char_p, _sz]),
     "gbfft_dftG": (_i, [_i, _i64p, _i, _vp, _vp, _vp, _vp]),
     "gbfft_dftGS": (_i, [_i, _i64p, _i, _i64, _vp, _vp, _vp, _vp]),
+    "gbfft_centre": (_i, [_i, _i64p, _i, _vp, _vp, _vp]),
+    "gbfft_shift": (_i, [_i, _i64p, _i, _i, _vp, _vp, _vp]),
     "gbfft_tune_load": (_i, [ctypes.c_char_p]),
     "gbfft_tune_clear": (_i, []),
     "gbfft_tune_count": (_i, []),

@@ -79,18 +79,28 @@ class Plan:
                 "gbfft_plan_create%s" % (self.shape,))
         self.handle = h
 
-    def exec_ptr(self, mode, in_ptr, out_ptr, stream=None):
+    def exec_ptr(self, mode, in_ptr, out_ptr, stream=None, opts=0):
+        if opts:
+            L.check(L.lib().gbfft_exec_ex(self.handle, mode_code(mode), ctypes.c_void_p(in_ptr),
+                                          ctypes.c_void_p(out_ptr), _stream(stream), int(opts)), "gbfft_exec_ex")
+            return
         L.check(L.lib().gbfft_exec(self.handle, mode_code(mode), ctypes.c_void_p(in_ptr),
                                    ctypes.c_void_p(out_ptr), _stream(stream)), "gbfft_exec")
 
-    def __call__(self, mode, x, out=None, stream=None):
+    def __call__(self, mode, x, out=None, stream=None, centre_in=False, shift_out=None):
+        """Transform x.  centre_in multiplies the input by (-1)^(sum of
+        indices) first; shift_out="shift" / "ishift" rolls the result like
+        shiftND / ishiftND (Centre.hs:36-164) -- both fused into the passes
+        where the lengths allow (gbfft_exec_ex)."""
         if not x.is_cuda or not x.is_contiguous():
             raise ValueError("gbfft: contiguous CUDA tensor required")
         if tuple(x.shape) != self.shape or x.dtype != self.dtype:
             raise ValueError("gbfft: tensor does not match the plan")
         if out is None:
             out = torch.empty_like(x)
-        self.exec_ptr(mode, x.data_ptr(), out.data_ptr(), stream)
+        opts = (L.OPT_CENTRE_IN if centre_in else 0) | {None: 0, "shift": L.OPT_SHIFT_OUT,
+                                                       "ishift": L.OPT_ISHIFT_OUT}[shift_out]
+        self.exec_ptr(mode, x.data_ptr(), out.data_ptr(), stream, opts)
         return out
 
     @property
@@ -214,6 +224,26 @@ def dft(arr, stream=None):
 def idft(arr, stream=None):
     """Math.DFT.idft (DFT.hs:44-53): dftG with inverseRootsOfUnity, then / n."""
     return dftG(roots_of_unity(arr.shape, True, arr.dtype, arr.device), arr, stream) / arr.shape[-1]
+
+
+def centre(arr, stream=None):
+    """Math.DFT.Centre.centre1D/2D/3D (Centre.hs:36-67): (-1)^(sum of indices) * arr."""
+    x = arr.contiguous()
+    out = torch.empty_like(x)
+    L.check(L.lib().gbfft_centre(x.dim(), _dims(x.shape), _dtype_code(x), ctypes.c_void_p(x.data_ptr()),
+                                 ctypes.c_void_p(out.data_ptr()), _stream(stream)), "gbfft_centre")
+    return out
+
+
+def shift(arr, inverse=False, stream=None):
+    """Math.DFT.Centre.shift1D/2D/3D, or ishift*D with inverse=True
+    (Centre.hs:70-164): roll every axis by n/2 (+1 for odd n when shifting)."""
+    x = arr.contiguous()
+    out = torch.empty_like(x)
+    L.check(L.lib().gbfft_shift(x.dim(), _dims(x.shape), _dtype_code(x), 1 if inverse else 0,
+                                ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()), _stream(stream)),
+            "gbfft_shift")
+    return out
 
 
 def ragged_autotune(lengths, modes, offsets=None, dtype=torch.complex64, stream=None):

@@ -170,6 +170,29 @@ int gbfft_dftG(int rank, const int64_t* dims, int dtype, const void* d_roots, co
 int gbfft_dftGS(int rank, const int64_t* dims, int dtype, int64_t k, const void* d_roots, const void* d_in,
                 void* d_out, void* stream);
 
+/* ---- fused centring / shifting: Math.DFT.Centre around a full transform --
+ * gbfft_exec_ex = gbfft_exec followed or preceded by Centre.hs helpers
+ * (DFT/Centre.hs:36-164), for FULL plans of rank 1..3:
+ *   GBFFT_OPT_SHIFT_OUT  / GBFFT_OPT_ISHIFT_OUT: shiftND / ishiftND of the
+ *     result, fused into the last pass of every axis as an index rotation;
+ *   GBFFT_OPT_CENTRE_IN: centreND of the input -- for even extents fused the
+ *     same way (centring the input rotates the output by n/2), otherwise one
+ *     extra pass before the transform.
+ * Axes whose last pass cannot rotate (a strided four-step axis) fall back to
+ * one shift pass after the transform (a stream-ordered temporary).  No
+ * counterpart in the reference's foreign path. */
+enum { GBFFT_OPT_SHIFT_OUT = 1, GBFFT_OPT_ISHIFT_OUT = 2, GBFFT_OPT_CENTRE_IN = 4 };
+int gbfft_exec_ex(const gbfft_plan* plan, int mode, const void* d_in, void* d_out, void* stream, int opts);
+
+/* ---- Math.DFT.Centre (DFT/Centre.hs:36-164), rank 1..3 ------------------
+ * gbfft_centre: centre1D/2D/3D, out = (-1)^(sum of the indices) * in (d_in
+ * may equal d_out).  gbfft_shift: shift1D/2D/3D (inverse = 0, roll by
+ * n/2 + (n odd) per axis) or ishift1D/2D/3D (inverse = 1, roll by n/2):
+ * out(ix) = in((ix + s) mod n) per axis; out-of-place.  One pass each. */
+int gbfft_centre(int rank, const int64_t* dims, int dtype, const void* d_in, void* d_out, void* stream);
+int gbfft_shift(int rank, const int64_t* dims, int dtype, int inverse, const void* d_in, void* d_out,
+                void* stream);
+
 /* ---- ragged batch: new beyond the reference API -------------------------
  * `count` independent 1D transforms of uneven lengths over one flat buffer,
  * executed by one persistent launch (the reference can only express this as

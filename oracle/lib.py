@@ -4,8 +4,9 @@ Functions mirror accelerate-fft's API: ``fft`` (innermost axis, FFT.hs:63-84),
 ``fft1D`` / ``fft2D`` / ``fft3D`` (FFT.hs:92-173) with Mode Forward / Reverse /
 Inverse, in the precision of the input (complex64 -> Float, complex128 ->
 Double); plus ``dft_naive`` (an FP64 per-row DFT), ``dftG`` / ``dftGS`` and
-``roots_of_unity`` as the reference writes them (DFT.hs:68-111, Roots.hs:26-51)
-and ``ceiling5_smooth`` (Adhoc.hs:289-313).
+``roots_of_unity`` as the reference writes them (DFT.hs:68-111, Roots.hs:26-51),
+``centre`` / ``shift`` (Centre.hs:36-164) and ``ceiling5_smooth``
+(Adhoc.hs:289-313).
 """
 import ctypes
 import os
@@ -138,6 +139,25 @@ def dftGS(k, roots, x):
     if lib().oracle_dftgs_f64(int(k), rows, l, roots.ctypes.data, x.ctypes.data, out.ctypes.data) != 0:
         raise ValueError("oracle: bad arguments for dftGS")
     return out[0]
+
+
+def centre(x):
+    """centre1D/2D/3D (Centre.hs:36-67): element ix times (-1) ** (sum of ix)."""
+    x = np.asarray(x)
+    idx = np.indices(x.shape).sum(axis=0)
+    return np.where(idx % 2 == 0, x, -x).astype(x.dtype)
+
+
+def shift(x, inverse=False):
+    """shift1D/2D/3D and ishift1D/2D/3D (Centre.hs:70-164): backpermute with
+    index (i + s) mod n per axis, s = n `quot` 2 + (odd n) for shift, n `quot` 2
+    for ishift."""
+    x = np.asarray(x)
+    out = x
+    for ax, n in enumerate(x.shape):
+        s = n // 2 + (0 if inverse else n % 2)
+        out = np.take(out, (np.arange(n) + s) % n, axis=ax)
+    return out
 
 
 def ceiling5_smooth(n):

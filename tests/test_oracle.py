@@ -135,3 +135,19 @@ def test_reference_properties(dtype, dim, gen, full, inner):
         d1 = np.sum(fx.astype(np.complex128) * np.conj(fy), axis=-1)
         d2 = n * np.sum(x.astype(np.complex128) * np.conj(y), axis=-1)
         assert rel_l2(d1, d2) < 10 * tol
+
+
+def test_centre_and_shift_restatement():
+    """Centre.hs restated: shift then ishift is the identity, and for even
+    lengths centring before a DFT equals shifting after it."""
+    import numpy as np
+    from oracle import lib as O
+    rng = np.random.default_rng(60)
+    for shape in [(8,), (7,), (4, 6), (5, 3), (2, 4, 6), (3, 5, 7)]:
+        x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+        assert np.array_equal(O.shift(O.shift(x), inverse=True), x)
+        if all(n % 2 == 0 for n in shape):
+            assert np.allclose(np.fft.fftn(O.centre(x)), O.shift(np.fft.fftn(x)), atol=1e-9)
+    assert np.array_equal(O.centre(np.ones(5)), np.array([1, -1, 1, -1, 1.0]))
+    assert np.array_equal(O.shift(np.arange(5)), np.array([3, 4, 0, 1, 2]))
+    assert np.array_equal(O.shift(np.arange(5), inverse=True), np.array([2, 3, 4, 0, 1]))
