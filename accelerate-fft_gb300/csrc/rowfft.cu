@@ -237,7 +237,8 @@ template <int N, int E, int ROWS, int MINB, int... Rs>
 __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_tma_kernel(const PassDesc d) {
   using C = float2;
   constexpr int TH = N / E;
-  constexpr int CH = ROWS * N;
+  constexpr int P = row_pitch<N>();  // slot pitch: the exchanges' swizzle spans whole 16-element blocks
+  constexpr int CH = ROWS * P;
   constexpr int R0 = rl_first(RL<Rs...>{});
   constexpr int RZ = rl_last(RL<Rs...>{});
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -258,7 +259,13 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_tma_kernel(const Pa
     const int64_t nr = (rows - r0 < ROWS) ? rows - r0 : ROWS;
     const uint32_t bytes = uint32_t(nr * N * sizeof(C));
     mbar_expect_tx(&bars[b], bytes);
-    tma_load_1d(buf0 + b * CH, in + r0 * N, bytes, &bars[b]);
+    if constexpr (P == N) {
+      tma_load_1d(buf0 + b * CH, in + r0 * N, bytes, &bars[b]);
+    } else {
+      // one copy per row into its pitched slot (N * 8 bytes, a multiple of 16)
+      for (int j = 0; j < int(nr); ++j)
+        tma_load_1d(buf0 + b * CH + j * P, in + (r0 + j) * N, uint32_t(N * sizeof(C)), &bars[b]);
+    }
   };
 
   if (threadIdx.x == 0) {
@@ -281,7 +288,7 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_tma_kernel(const Pa
     // the abort decision is made uniformly across the CTA
     const bool timed_out = !mbar_wait_bounded(&bars[b], par, d.status);
     if (__syncthreads_or(timed_out)) break;
-    C* sb = buf0 + b * CH + slot * N;
+    C* sb = buf0 + b * CH + slot * P;
     const int64_t row = c * ROWS + slot;
     const bool ok = row < rows;
     C v[E];
@@ -602,7 +609,8 @@ int RowTcCfg<N, ROWS, MINB, Rs...>::ctas_per_sm = 1;
 template <typename T, int N, int E, int ROWS, int MINB, int... Rs>
 struct RowCfg {
   static constexpr int threads = ROWS * (N / E);
-  static constexpr bool tma_capable = sizeof(T) == 4 && N % 16 == 0;
+  // bulk copies move whole rows: N * 8 bytes must be a multiple of 16
+  static constexpr bool tma_capable = sizeof(T) == 4 && N % 2 == 0;
   static size_t smem() { return size_t(2) * ROWS * row_pitch<N>() * sizeof(typename CxT<T>::type); }
   [[maybe_unused]] static int tma_ctas_per_sm;
   static constexpr int MINB1 = (MINB >= 3 && sizeof(T) == 4) ? 4 : MINB;

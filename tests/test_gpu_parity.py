@@ -333,7 +333,8 @@ def test_kernel_variants_agree(gbfft_lib, monkeypatch, disable, rowv, colv):
     monkeypatch.setenv("GBFFT_COL_VARIANT", colv)
     rng = np.random.default_rng(99)
     cases = [((4096, 4096), "full", np.complex64), ((300, 1024), "many", np.complex64),
-             ((64, 1000), "many", np.complex64), ((5, 8192), "many", np.complex64),
+             ((64, 1000), "many", np.complex64), ((67, 1000), "many", np.complex64),
+             ((5, 8192), "many", np.complex64),
              ((41, 256), "many", np.complex64), ((3, 2048), "full", np.complex64),
              ((7, 512), "many", np.complex64), ((33, 4096), "many", np.complex128),
              ((2, 4096, 32), "full", np.complex64), ((256, 48), "full", np.complex64),
