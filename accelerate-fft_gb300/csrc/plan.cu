@@ -888,7 +888,10 @@ int build_plan(gbfft_plan* p, bool dry) {
     // GB300); GBFFT_DISABLE=tma turns every one off for A/B checks
     const int want = ps.d.kernel == K_ROW ? tc.row_tma : ps.d.kernel == K_STRIDED ? tc.str_tma : 1;
     ps.d.use_tma = (tma && want) ? 1 : 0;
-    ps.d.row_variant = tc.row_variant;
+    // untuned: Complex Float register rows double-buffered (measured faster
+    // at every length); Complex Double rows single-buffered (half the shared
+    // memory per CTA); tensor-core rows at their lower CTAs-per-SM bound
+    ps.d.row_variant = tc.row_variant >= 0 ? tc.row_variant : (ps.d.kernel == K_ROW && !p->dbl) ? 0 : 1;
     ps.d.col_variant = tc.col_variant;
     if (const char* rv = std::getenv("GBFFT_ROW_VARIANT")) ps.d.row_variant = std::atoi(rv) & 1;
     if (const char* cv = std::getenv("GBFFT_COL_VARIANT")) ps.d.col_variant = std::atoi(cv) & 15;

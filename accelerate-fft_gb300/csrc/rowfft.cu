@@ -655,15 +655,20 @@ template <typename T, int N, int E, int ROWS, int MINB, int... Rs>
 int RowCfg<T, N, E, ROWS, MINB, Rs...>::tma_ctas_per_sm = 1;
 
 // The specialised lengths (type, N, E, rows per CTA, min CTAs per SM,
-// radices = factor_device(N)).
+// radices = factor_device(N)).  Rows per CTA are chosen small and CTAs per
+// SM high, so some CTAs load while others compute: measured on GB300 with
+// the double-buffered kernel (milliseconds for 512 MiB of rows),
+//   256: 16 rows x 3 CTAs 0.169, 8 x 5 0.161    512: 0.187 -> 0.177
+//  1024: 0.201 -> 0.189                        2048: 0.210 -> 0.191
+//  1000 (100 threads a row): 4 rows x 2 CTAs 0.251, 2 x 5 (56 registers) 0.203.
 #define GBFFT_ROW_TABLE(X)                   \
-  X(float, 256, 16, 16, 3, 16, 16)           \
-  X(float, 512, 16, 8, 3, 16, 16, 2)         \
-  X(float, 1024, 16, 4, 3, 16, 16, 4)        \
-  X(float, 2048, 16, 2, 3, 16, 16, 8)        \
+  X(float, 256, 16, 8, 5, 16, 16)            \
+  X(float, 512, 16, 4, 5, 16, 16, 2)         \
+  X(float, 1024, 16, 2, 5, 16, 16, 4)        \
+  X(float, 2048, 16, 1, 5, 16, 16, 8)        \
   X(float, 4096, 16, 1, 3, 16, 16, 16)       \
   X(float, 8192, 16, 1, 1, 16, 16, 16, 2)    \
-  X(float, 1000, 10, 4, 2, 10, 10, 10)       \
+  X(float, 1000, 10, 2, 5, 10, 10, 10)       \
   X(double, 256, 16, 16, 2, 16, 16)          \
   X(double, 512, 16, 8, 2, 16, 16, 2)        \
   X(double, 1024, 16, 4, 2, 16, 16, 4)       \

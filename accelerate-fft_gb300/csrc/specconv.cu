@@ -333,8 +333,8 @@ int gbfft_specconv_plan_create(gbfft_specconv_plan** out, int64_t batch, int64_t
   unsigned char* tb = static_cast<unsigned char*>(p->d_tables);
   for (PassSpec* ps : {&p->px, &p->py, &p->pz, &p->pzb}) {
     if (ps->tw_off >= 0) ps->d.tw = tb + ps->tw_off;
-    ps->d.use_tma = 1;
-    ps->d.row_variant = 1;
+    ps->d.use_tma = ps->d.kernel == K_ROW ? 0 : 1;  // rows: register kernel, double-buffered
+    ps->d.row_variant = dbl ? 1 : 0;
     ps->d.col_variant = 9;
   }
   p->tmp_bytes = size_t(batch) * size_t(p->N) * (dbl ? 16 : 8);
