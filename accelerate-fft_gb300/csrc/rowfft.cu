@@ -691,12 +691,14 @@ struct RowBlueCfg {
 };
 
 // one-pass Bluestein rows: (type, padded length N, E, rows per CTA, min CTAs
-// per SM, radices = factor_device(N))
+// per SM, radices = factor_device(N)).  2048 (rows of 1009): one row per
+// CTA and three CTAs per SM ran 16384 rows in 0.187 ms against 0.212 ms
+// for two rows and two CTAs.
 #define GBFFT_ROWBLUE_TABLE(X)              \
   X(float, 256, 16, 16, 2, 16, 16)          \
   X(float, 512, 16, 8, 2, 16, 16, 2)        \
   X(float, 1024, 16, 4, 2, 16, 16, 4)       \
-  X(float, 2048, 16, 2, 2, 16, 16, 8)       \
+  X(float, 2048, 16, 1, 3, 16, 16, 8)       \
   X(float, 4096, 16, 1, 2, 16, 16, 16)
 
 int g_sms = 0;
