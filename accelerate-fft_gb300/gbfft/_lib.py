@@ -39,6 +39,7 @@ SIGNATURES = {
     "gbfft_plan_destroy": (_i, [_vp]),
     "gbfft_exec": (_i, [_vp, _i, _vp, _vp, _vp]),
     "gbfft_exec_ex": (_i, [_vp, _i, _vp, _vp, _vp, _i]),
+    "gbfft_probe_tile_copy": (_i, [_i64, _i64, _i, _vp, _vp, _vp]),
     "gbfft_plan_get": (_i, [ctypes.POINTER(_vp), _i, _i64p, _i, _i, _i]),
     "gbfft_fft": (_i, [_i, _i, _i64p, _i, _i, _vp, _vp, _vp]),
     "gbfft_cache_clear": (_i, []),

@@ -354,6 +354,36 @@ def run_gbfft(args, wl):
     ach = bytes_pass / (avg_pass[dom] * 1e-3) / 1e9 if nlaunch else 0.0
     ach_tr = bytes_pass * len(ops) / (ms * 1e-3) / 1e9
 
+    # the access pattern's own ceiling (outside the timed region): a plain
+    # copy of the same array in 16-column tiles over all rows -- what a
+    # strided pass moving 16-column tiles cannot beat -- and the contiguous
+    # copy of a row pass
+    ceiling = None
+    if rank == 0 and wl["kind"] == "full" and len(shape) >= 2 and elem == 8 and nlaunch:
+        rows, cols = shape[0], nelem // shape[0]
+        gbs = {}
+        for w in (16, cols):
+            for _ in range(3):
+                L.check(lib.gbfft_probe_tile_copy(rows, cols, w, ctypes.c_void_p(x.data_ptr()),
+                                                  ctypes.c_void_p(z.data_ptr()), sp), "gbfft_probe_tile_copy")
+            ts = []
+            for k in range(10):
+                flush.fill_(float(k))
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                L.check(lib.gbfft_probe_tile_copy(rows, cols, w, ctypes.c_void_p(x.data_ptr()),
+                                                  ctypes.c_void_p(z.data_ptr()), sp), "gbfft_probe_tile_copy")
+                b.record(stream)
+                torch.cuda.synchronize()
+                ts.append(a.elapsed_time(b))
+            gbs[w] = bytes_pass / (statistics.median(ts) * 1e-3) / 1e9
+        rel = gbs[cols] if kernels[dom].startswith("row") else gbs[16]
+        ceiling = {"kernel": kernels[dom], "tile16_copy_gbs": gbs[16], "contiguous_copy_gbs": gbs[cols],
+                   "frac_of_pattern": ach / rel,
+                   "note": "gbfft_probe_tile_copy over the %dx%d array: 16-column tiles (the strided passes' "
+                           "pattern) and whole rows; frac_of_pattern = achieved / the copy of the dominant "
+                           "kernel's pattern" % (rows, cols)}
+
     # accuracy of one result vs FP64 (numpy pocketfft), outside the timed region
     rel_err = None
     roundtrip_err = None
@@ -502,7 +532,8 @@ def run_gbfft(args, wl):
                          "peak_source": peak_kind,
                          "kernel": "pass %d of %d (%s)" % (dom, npass, kernels[dom] if npass else "-"),
                          "bytes_alg_per_launch": bytes_pass,
-                         "kernel_ms": avg_pass[dom] if npass else None},
+                         "kernel_ms": avg_pass[dom] if npass else None,
+                         "pattern_ceiling": ceiling},
             "roofline_transform": {"achieved": ach_tr, "frac": ach_tr / peak, "kernels": kernels,
                                    "bytes_alg": bytes_pass, "pass_ms": avg_pass},
             "rel_err_vs_fp64": rel_err,

@@ -475,3 +475,25 @@ def test_fft_rank4_and_5(gbfft_lib, shape):
     L.lib().gbfft_plan_destroy(h)
     assert L.lib().gbfft_plan_create(ctypes.byref(h), len(shape), dims, L.KIND_FULL, L.C32,
                                      L.PLAIN) == L.ERR_UNSUPPORTED
+
+
+def test_probe_tile_copy(gbfft_lib):
+    """The bandwidth probe of the strided passes' access pattern copies the
+    array exactly at every tile width, and refuses widths that do not tile."""
+    from gbfft import _lib as L
+    import ctypes
+    x = torch.randn(300, 256, dtype=torch.complex64, device="cuda")
+    for w in (2, 16, 64, 256):
+        y = torch.zeros_like(x)
+        assert L.lib().gbfft_probe_tile_copy(300, 256, w, ctypes.c_void_p(x.data_ptr()),
+                                             ctypes.c_void_p(y.data_ptr()), None) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(x, y), w
+    big = torch.randn(4, 16384, dtype=torch.complex64, device="cuda")
+    y = torch.zeros_like(big)
+    assert L.lib().gbfft_probe_tile_copy(4, 16384, 16384, ctypes.c_void_p(big.data_ptr()),
+                                         ctypes.c_void_p(y.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(big, y)
+    assert L.lib().gbfft_probe_tile_copy(300, 256, 24, ctypes.c_void_p(x.data_ptr()),
+                                         ctypes.c_void_p(y.data_ptr()), None) == L.ERR_INVALID_ARG
