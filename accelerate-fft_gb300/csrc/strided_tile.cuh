@@ -331,6 +331,24 @@ __device__ __forceinline__ void str_finish(const PassDesc& d, const StrCtx& c,
     e.y *= s * csign_out;
     return true;
   };
+  // the same with 32-bit index arithmetic: the four-step exponent
+  // (column or batch) * k below 2^32, the axis index l below 2^31
+  auto post32 = [&](C& e, uint32_t k, uint32_t cl) -> bool {
+    uint32_t l = 0;
+    if constexpr ((OPS & (F_FILTER_OUT | F_CHIRP_OUT | F_BLUE | F_TRUNC_OUT)) != 0) {
+      l = k * uint32_t(d.lout_es) + cl * uint32_t(d.lout_cs);
+      if ((OPS & F_TRUNC_OUT) && int64_t(l) >= d.n_out) return false;
+    }
+    if constexpr ((OPS & F_TW4) != 0) {
+      const uint32_t tt = ((OPS & F_TW4_BATCH) ? uint32_t(b_lo) : cl) * k;
+      e = cmul(e, cmul(tw4_hi[tt >> tw4_shift], tw4_lo[tt & uint32_t(tw4_mask)]));
+    }
+    if constexpr ((OPS & F_FILTER_OUT) != 0) e = cconj(cmul(e, filt[l]));
+    if constexpr ((OPS & (F_BLUE | F_CHIRP_OUT)) != 0) e = cmul(cconj(e), chirp[l]);
+    e.x *= s;
+    e.y *= s * csign_out;
+    return true;
+  };
   if (d.out_cs == 1 && !d.col_out_off) {
     if (!ok) return;
     C* o0 = out + col + int64_t(t) * oes;
@@ -363,6 +381,34 @@ __device__ __forceinline__ void str_finish(const PassDesc& d, const StrCtx& c,
         b[k * W + (x ^ (k & (W - 1)))] = v[q * RZ + r];
       }
     __syncthreads();
+    // 32-bit offsets and exponents when the tile allows (no per-column
+    // offsets, no rotation, every product in range): the common case
+    const int64_t clast = c0 + W - 1;
+    const int64_t lim31 = int64_t(1) << 31;
+    const bool small = !d.col_out_off && !(d.flags & F_ROT_OUT) &&
+                       int64_t(W - 1) * d.out_cs + int64_t(N - 1) * oes < lim31 &&
+                       clast * d.lout_cs + int64_t(N - 1) * d.lout_es < lim31 &&
+                       ((OPS & F_TW4) == 0 ||
+                        ((OPS & F_TW4_BATCH) ? b_lo : clast) * int64_t(N - 1) < (int64_t(1) << 32)) &&
+                       clast < lim31;
+    if (small) {
+      C* __restrict__ ob = out + c0 * d.out_cs;
+      const int ocs = int(d.out_cs), oes32 = int(oes);
+      const int cmax = int(d.ncols - c0 < W ? d.ncols - c0 : W);
+#pragma unroll 4
+      for (int f = threadIdx.x; f < N * W; f += W * TH) {
+        const int cc = f / N, k = f % N;
+        if (cc >= cmax) continue;
+        C e = b[k * W + (cc ^ (k & (W - 1)))];
+        if (!post32(e, uint32_t(k), uint32_t(c0 + cc))) continue;
+        C* o = ob + (cc * ocs + k * oes32);
+        if (keep)
+          st_l2hint(o, e, pol);
+        else
+          *o = e;
+      }
+      return;
+    }
 #pragma unroll 4
     for (int f = threadIdx.x; f < N * W; f += W * TH) {
       const int cc = f / N, k = f % N;
