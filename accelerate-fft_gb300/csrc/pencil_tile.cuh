@@ -187,7 +187,8 @@ __device__ __forceinline__ void pencil_store(const PassDesc& d, typename CxT<T>:
   C* __restrict__ base = out + (d.col_out_off ? 0 : c0 * d.out_cs);
   for (int f0 = threadIdx.x; f0 < total; f0 += KU * step) {
     C v[KU];
-    int64_t lidx[KU], tt[KU], cofs[KU];
+    int64_t lidx[KU], cofs[KU];
+    uint32_t tt[KU];  // four-step exponent: column (or batch) * k < n <= 2^26
     I ofs[KU];
     bool ok[KU];
 #pragma unroll
@@ -211,7 +212,7 @@ __device__ __forceinline__ void pencil_store(const PassDesc& d, typename CxT<T>:
       ok[u] = valid;
       lidx[u] = valid ? l : 0;
       // e < N/n and kk < n, so the four-step exponent stays below N
-      tt[u] = (valid && (fl & F_TW4)) ? ((fl & F_TW4_BATCH) ? b : col) * int64_t(kk) : 0;
+      tt[u] = (valid && (fl & F_TW4)) ? uint32_t((fl & F_TW4_BATCH) ? b : col) * uint32_t(kk) : 0u;
       v[u] = valid ? res[c * d.pitch + spad(kk)] : cmake<C>(T(0), T(0));
       ofs[u] = I(kk) * oes + (d.col_out_off ? I(0) : I(c) * ocs);
       cofs[u] = (d.col_out_off && valid) ? d.col_out_off[col] : 0;
@@ -221,7 +222,7 @@ __device__ __forceinline__ void pencil_store(const PassDesc& d, typename CxT<T>:
 #pragma unroll
       for (int u = 0; u < KU; ++u) {
         wh[u] = tw4_hi[tt[u] >> d.tw4_shift];
-        wl[u] = tw4_lo[tt[u] & tw4_mask];
+        wl[u] = tw4_lo[tt[u] & uint32_t(tw4_mask)];
       }
 #pragma unroll
       for (int u = 0; u < KU; ++u) v[u] = cmul(v[u], cmul(wh[u], wl[u]));

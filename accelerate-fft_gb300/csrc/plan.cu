@@ -240,6 +240,9 @@ bool Builder::stages_for(int n, PassSpec& ps) {
   return true;
 }
 
+// Four-step twiddle tables W_N^t = hi[t >> shift] * lo[t & mask].  N is a
+// four-step length n1 * n2 with both halves at most the tile cap (8192),
+// so N <= 2^26 and the exponents t < N fit the kernels' 32-bit arithmetic.
 void Builder::tw4_for(int64_t N, PassSpec& ps) {
   int shift = 0;
   while ((int64_t(1) << (2 * shift)) < N) ++shift;
