@@ -53,14 +53,20 @@ __global__ void __launch_bounds__(kProbeThreads) tile_copy_kernel(const float4* 
 extern "C" int gbfft_probe_tile_copy(int64_t rows, int64_t cols, int width, const void* in, void* out,
                                      void* stream) {
   using namespace gbfft;
-  if (rows < 1 || cols < 2 || width < 2 || (width & (width - 1)) || cols % width || cols % 2 ||
-      rows > (int64_t(1) << 40) / cols)
+  if (rows < 1 || cols < 2 || width < 2 || width % 2 || cols % width || rows > (int64_t(1) << 40) / cols)
     return GBFFT_ERR_INVALID_ARG;
   if (!in || !out || in == out ||
       ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15))
     return GBFFT_ERR_INVALID_ARG;
-  // segments above 8192 columns are contiguous runs of 64 KiB either way
-  const int seg = std::min(width / 2, 4096);
+  // segments above 8192 columns are copied as contiguous runs of at most
+  // 64 KiB (a divisor of the segment), the same access pattern
+  int seg = width / 2;
+  if (seg > 4096) {
+    int best = 1;
+    for (int dv = 1; dv <= 4096; ++dv)
+      if ((width / 2) % dv == 0) best = dv;
+    seg = best;
+  }
   const int rs = std::max(1, 4096 / seg);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);

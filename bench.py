@@ -359,10 +359,12 @@ def run_gbfft(args, wl):
     # strided pass moving 16-column tiles cannot beat -- and the contiguous
     # copy of a row pass
     ceiling = None
-    if rank == 0 and wl["kind"] == "full" and len(shape) >= 2 and elem == 8 and nlaunch:
-        rows, cols = shape[0], nelem // shape[0]
+    full2 = wl["kind"] == "full" and len(shape) >= 2
+    rowsv = wl["kind"] == "many" and len(shape) >= 2 and shape[-1] % 2 == 0
+    if rank == 0 and (full2 or rowsv) and elem == 8 and nlaunch:
+        rows, cols = (shape[0], nelem // shape[0]) if full2 else (nelem // shape[-1], shape[-1])
         gbs = {}
-        for w in (16, cols):
+        for w in ((16, cols) if full2 else (cols,)):
             for _ in range(3):
                 L.check(lib.gbfft_probe_tile_copy(rows, cols, w, ctypes.c_void_p(x.data_ptr()),
                                                   ctypes.c_void_p(z.data_ptr()), sp), "gbfft_probe_tile_copy")
@@ -377,12 +379,14 @@ def run_gbfft(args, wl):
                 torch.cuda.synchronize()
                 ts.append(a.elapsed_time(b))
             gbs[w] = bytes_pass / (statistics.median(ts) * 1e-3) / 1e9
-        rel = gbs[cols] if kernels[dom].startswith("row") else gbs[16]
-        ceiling = {"kernel": kernels[dom], "tile16_copy_gbs": gbs[16], "contiguous_copy_gbs": gbs[cols],
-                   "frac_of_pattern": ach / rel,
-                   "note": "gbfft_probe_tile_copy over the %dx%d array: 16-column tiles (the strided passes' "
-                           "pattern) and whole rows; frac_of_pattern = achieved / the copy of the dominant "
-                           "kernel's pattern" % (rows, cols)}
+        row_kernel = kernels[dom].startswith("row")
+        rel = gbs[cols] if row_kernel else gbs.get(16)
+        ceiling = {"kernel": kernels[dom], "tile16_copy_gbs": gbs.get(16), "contiguous_copy_gbs": gbs[cols],
+                   "frac_of_pattern": ach / rel if rel else None,
+                   "note": "gbfft_probe_tile_copy over the %dx%d array: %s; frac_of_pattern = achieved / the "
+                           "copy of the dominant kernel's pattern" % (
+                               rows, cols, "16-column tiles (the strided passes' pattern) and whole rows"
+                               if full2 else "whole rows (the row kernels' pattern)")}
 
     # accuracy of one result vs FP64 (numpy pocketfft), outside the timed region
     rel_err = None

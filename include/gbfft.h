@@ -139,8 +139,8 @@ int gbfft_plan_pass_kernel(const gbfft_plan* plan, int pass, char* buf, size_t c
  * copies a rows x cols Complex Float array `in` to `out` in tiles of `width`
  * contiguous columns over all rows -- the access pattern of a strided pass
  * with W = width (width = cols: the contiguous pattern of a row pass).
- * width a power of two >= 2 dividing cols (widths above 8192 copy 8192-
- * column runs, which are contiguous all the same); 16-byte aligned buffers. */
+ * width even and dividing cols (widths above 8192 copy runs of at most
+ * 8192 columns, contiguous all the same); 16-byte aligned buffers. */
 int gbfft_probe_tile_copy(int64_t rows, int64_t cols, int width, const void* in, void* out, void* stream);
 
 /* ---- autotuner: new beyond the reference API ---------------------------

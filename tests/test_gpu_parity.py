@@ -478,8 +478,9 @@ def test_fft_rank4_and_5(gbfft_lib, shape):
 
 
 def test_probe_tile_copy(gbfft_lib):
-    """The bandwidth probe of the strided passes' access pattern copies the
-    array exactly at every tile width, and refuses widths that do not tile."""
+    """The bandwidth probe of the passes' access patterns copies the array
+    exactly at every tile width (powers of two, whole rows of 1000, runs of a
+    24000-column row), and refuses widths that do not tile."""
     from gbfft import _lib as L
     import ctypes
     x = torch.randn(300, 256, dtype=torch.complex64, device="cuda")
@@ -495,5 +496,19 @@ def test_probe_tile_copy(gbfft_lib):
                                          ctypes.c_void_p(y.data_ptr()), None) == 0
     torch.cuda.synchronize()
     assert torch.equal(big, y)
-    assert L.lib().gbfft_probe_tile_copy(300, 256, 24, ctypes.c_void_p(x.data_ptr()),
-                                         ctypes.c_void_p(y.data_ptr()), None) == L.ERR_INVALID_ARG
+    rows = torch.randn(64, 1000, dtype=torch.complex64, device="cuda")
+    y = torch.zeros_like(rows)
+    assert L.lib().gbfft_probe_tile_copy(64, 1000, 1000, ctypes.c_void_p(rows.data_ptr()),
+                                         ctypes.c_void_p(y.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(rows, y)
+    wide = torch.randn(3, 2 * 12000, dtype=torch.complex64, device="cuda")
+    y = torch.zeros_like(wide)
+    assert L.lib().gbfft_probe_tile_copy(3, 24000, 24000, ctypes.c_void_p(wide.data_ptr()),
+                                         ctypes.c_void_p(y.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(wide, y)
+    y = torch.zeros_like(x)
+    for bad in (24, 3, 0):
+        assert L.lib().gbfft_probe_tile_copy(300, 256, bad, ctypes.c_void_p(x.data_ptr()),
+                                             ctypes.c_void_p(y.data_ptr()), None) == L.ERR_INVALID_ARG
