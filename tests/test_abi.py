@@ -100,3 +100,22 @@ def test_tune_file_parser(gbfft_lib, tmp_path):
     assert lib.gbfft_tune_load(str(tmp_path / "missing.jsonl").encode()) == 0
     lib.gbfft_tune_clear()
     assert lib.gbfft_tune_count() == 0
+
+
+def test_argument_checks_need_no_device(gbfft_lib):
+    """Entry points reject bad arguments before touching CUDA: the fused
+    centre/shift execution, the Centre.hs kernels and the bandwidth probe."""
+    from gbfft import _lib as L
+    lib = L.lib()
+    vp = ctypes.c_void_p
+    assert lib.gbfft_exec_ex(None, L.FORWARD, None, None, None, L.OPT_SHIFT_OUT) == L.ERR_NULL_PLAN
+    d3 = (ctypes.c_int64 * 4)(2, 3, 4, 5)
+    assert lib.gbfft_centre(4, d3, L.C32, vp(16), vp(32), None) == L.ERR_INVALID_ARG  # rank 1..3
+    assert lib.gbfft_centre(2, d3, 7, vp(16), vp(32), None) == L.ERR_INVALID_ARG  # element type
+    assert lib.gbfft_shift(2, d3, L.C32, 0, vp(16), vp(16), None) == L.ERR_INVALID_ARG  # in place
+    z = (ctypes.c_int64 * 2)(0, 5)
+    assert lib.gbfft_shift(2, z, L.C32, 1, None, None, None) == L.OK  # empty: nothing to do
+    assert lib.gbfft_probe_tile_copy(300, 256, 24, vp(16), vp(4096), None) == L.ERR_INVALID_ARG
+    assert lib.gbfft_probe_tile_copy(300, 256, 3, vp(16), vp(4096), None) == L.ERR_INVALID_ARG
+    assert lib.gbfft_probe_tile_copy(4, 4, 2, None, None, None) == L.ERR_INVALID_ARG
+    assert lib.gbfft_probe_tile_copy(4, 4, 2, vp(8), vp(4096), None) == L.ERR_INVALID_ARG  # 16-byte aligned
