@@ -888,8 +888,11 @@ int build_plan(gbfft_plan* p, bool dry) {
   for (PassSpec& ps : p->passes) {
     ps.d.status = p->d_status;
     // tensor / bulk copies per kernel kind as chosen (defaults: measured on
-    // GB300); GBFFT_DISABLE=tma turns every one off for A/B checks
-    const int want = ps.d.kernel == K_ROW ? tc.row_tma : ps.d.kernel == K_STRIDED ? tc.str_tma : 1;
+    // GB300); GBFFT_DISABLE=tma turns every one off for A/B checks,
+    // GBFFT_ROW_TMA=1 streams register rows by bulk copies
+    int row_tma = tc.row_tma;
+    if (const char* rt = std::getenv("GBFFT_ROW_TMA")) row_tma = std::atoi(rt) & 1;
+    const int want = ps.d.kernel == K_ROW ? row_tma : ps.d.kernel == K_STRIDED ? tc.str_tma : 1;
     ps.d.use_tma = (tma && want) ? 1 : 0;
     // untuned: Complex Float register rows double-buffered (measured faster
     // at every length); Complex Double rows single-buffered (half the shared

@@ -330,6 +330,7 @@ def test_kernel_variants_agree(gbfft_lib, monkeypatch, disable, rowv, colv):
     from gbfft import _lib as L
     monkeypatch.setenv("GBFFT_DISABLE", disable)
     monkeypatch.setenv("GBFFT_ROW_VARIANT", rowv)
+    monkeypatch.setenv("GBFFT_ROW_TMA", "1" if rowv == "0" else "0")  # bulk-copy-fed rows
     monkeypatch.setenv("GBFFT_COL_VARIANT", colv)
     rng = np.random.default_rng(99)
     cases = [((4096, 4096), "full", np.complex64), ((300, 1024), "many", np.complex64),
