@@ -1,11 +1,10 @@
 // Allocation-free batched 1D transform for callers that cannot allocate
 // device memory.
 //
-// Who needs it: a host that owns the device heap itself -- Accelerate's PTX
-// backend hands the FFI pre-allocated arrays from its own allocator and
-// expects the foreign call not to grab memory behind its back -- and code
-// recording a CUDA graph by stream capture, where cudaMalloc is not allowed.
-// This entry point runs Bluestein's algorithm (four pencil passes: chirp and
+// Who needs it: a host that owns the device heap itself.  Accelerate's PTX
+// backend hands the FFI pre-allocated arrays from its own allocator, keeps
+// its own accounting of device memory, and expects a foreign call not to grab
+// memory behind its back.  This entry point runs Bluestein's algorithm (four pencil passes: chirp and
 // forward four-step half; second half and filter; inverse first half; inverse
 // second half and chirp) for any length, and keeps everything the passes need
 // beyond the caller's input and output -- twiddle, chirp and filter tables and
@@ -13,11 +12,17 @@
 // kNoallocBytes.  It calls no cudaMalloc, cudaFree or other device allocator.
 //
 // Rules of use:
-//  * The array exists once per device that loads the library and lives
-//    until the process exits.
-//  * The first call on a device resolves the array's device address with
-//    cudaGetSymbolAddress (with that device current) and sets kernel
-//    attributes; make that first call before any stream capture.
+//  * The array exists once per device (once per CUDA context: a context
+//    that loads the library gets its own copy) and lives until the process
+//    exits.
+//  * Every call resolves the array's device address in the context that is
+//    current (cudaGetSymbolAddress; host code only holds a stand-in for the
+//    symbol), and the first call in a context also sets kernel attributes
+//    and uploads the tables; make that first call before any stream capture.
+//    The tables held in the array are tracked per context, keyed on the
+//    context's never-reused ID, so a caller that switches between contexts
+//    (Accelerate's PTX backend creates its own) never reuses the address or
+//    the tables of another context.
 //  * Every call shares the array and it keeps the last call's contents:
 //    tables are rewritten whenever the length changes, nothing relies on
 //    the work area starting at zero, and calls that overlap on the GPU (two
@@ -28,6 +33,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -40,19 +46,21 @@ namespace {
 constexpr size_t kNoallocBytes = size_t(16) << 20;  // 16 MiB per device
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
-constexpr int kMaxDevices = 64;
-
-struct DevState {
-  bool ready = false;
+// Per-context state: the array's address in that context and the tables
+// currently held at its head.
+struct CtxState {
   unsigned char* ptr = nullptr;  // device address of g_noalloc_scratch
   int64_t n = 0, m = 0;
   bool dbl = false;
   size_t tables_bytes = 0;
-  std::vector<PassSpec> passes;  // relative to the scratch base
+  std::vector<PassSpec> passes;  // pointing into the array
 };
 
 std::mutex g_mu;
-DevState g_dev[kMaxDevices];
+std::map<uint64_t, CtxState>& ctx_states() {
+  static auto* m = new std::map<uint64_t, CtxState>();
+  return *m;
+}
 
 // m = m1 * m2 with both factors within one CTA, m1 close to sqrt(m).
 bool split_m(int64_t m, int cap, int64_t& m1, int64_t& m2) {
@@ -171,29 +179,42 @@ extern "C" int gbfft_fft_noalloc(int mode, int64_t n, int64_t batch, int dtype, 
   }
   if (n > (int64_t(1) << 24)) return GBFFT_ERR_TOO_LARGE;
   const int64_t m = bluestein_length(n);
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return GBFFT_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxDevices) return GBFFT_ERR_UNSUPPORTED;
+  // the two work sequences alone must fit (checked before any table is built)
+  if (2 * double(batch) * double(m) * double(eb) > double(kNoallocBytes)) return GBFFT_ERR_TOO_LARGE;
+  // The array's address in the context current on this thread (resolving it
+  // also initialises the device's primary context when no context is
+  // current, so there is always a context to key the state on).
+  void* sym = nullptr;
+  if (cudaGetSymbolAddress(&sym, g_noalloc_scratch) != cudaSuccess || !sym) return GBFFT_ERR_CUDA;
+  const uint64_t ctx = current_context_id();
 
   std::lock_guard<std::mutex> lk(g_mu);
-  DevState& st = g_dev[dev];
-  if (!st.ready) {
-    // set-up, once per device, with that device current
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return GBFFT_ERR_CUDA;
-    if (prepare_kernels() != cudaSuccess) return GBFFT_ERR_CUDA;
-    st.ptr = static_cast<unsigned char*>(p);
-    st.ready = true;
+  CtxState& st = ctx_states()[ctx];
+  if (st.ptr != sym) {
+    // set-up, once per context, with that context current
+    if (prepare_kernels() != cudaSuccess) {
+      ctx_states().erase(ctx);
+      return GBFFT_ERR_CUDA;
+    }
+    st = CtxState();
+    st.ptr = static_cast<unsigned char*>(sym);
   }
   if (st.n != n || st.m != m || st.dbl != dbl || st.passes.empty()) {
+    // The table upload below copies from host memory that is freed on
+    // return; it is not recorded into a stream that is being captured.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return GBFFT_ERR_CUDA;
+    if (cap != cudaStreamCaptureStatusNone) return GBFFT_ERR_UNSUPPORTED;
     Builder B;
     B.dbl = dbl;
     std::vector<PassSpec> passes;
     const int rc = build_passes(B, n, 1, m, passes);
     if (rc != GBFFT_OK) return rc;
     const size_t tb = (B.blob.size() + 255) & ~size_t(255);
-    if (tb + 2 * size_t(m) * eb > kNoallocBytes) return GBFFT_ERR_TOO_LARGE;
-    // the tables go to the head of the array (a copy, not an allocation)
+    if (tb + 2 * size_t(batch) * size_t(m) * eb > kNoallocBytes) return GBFFT_ERR_TOO_LARGE;
+    // the tables go to the head of the array (a copy, not an allocation);
+    // the state is marked empty until the copy is enqueued
+    st.passes.clear();
     if (cudaMemcpyAsync(st.ptr, B.blob.data(), B.blob.size(), cudaMemcpyHostToDevice, s) != cudaSuccess)
       return GBFFT_ERR_CUDA;
     for (PassSpec& ps : passes) {

@@ -946,7 +946,9 @@ int build_split_plan(gbfft_plan* p) {
   bool any = false;
   for (PassSpec& ps : p->passes)
     if (tc_row(ps)) any = true;
-  if (!any) return GBFFT_OK;  // no radix-16 row pass: the plain kernels serve the plan
+  // A split-FP16 request is served by tensor-core passes or refused: a plan
+  // with no pass on the tensor cores would silently be the FP32 plan.
+  if (!any) return GBFFT_ERR_UNSUPPORTED;
   if (fault_injected("alloc")) return GBFFT_ERR_ALLOC;
   if (cudaMalloc(&p->d_tcmat, dm.size() * sizeof(__half)) != cudaSuccess) return GBFFT_ERR_ALLOC;
   if (cudaMemcpy(p->d_tcmat, dm.data(), dm.size() * sizeof(__half), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -1038,6 +1040,41 @@ int exec_passes(const gbfft_plan* p, const std::vector<PassSpec>& passes, int mo
     if (launch_pass(d, p->dbl, s) != cudaSuccess) return GBFFT_ERR_CUDA;
   }
   return GBFFT_OK;
+}
+
+// Identity of the CUDA context current on this thread: cuCtxGetId's ID,
+// which the driver never hands out twice in a process (a CUcontext handle of
+// a destroyed context can come back for a new one, an ID cannot).  Without a
+// current context (cannot happen after cudaFree(nullptr)) the device number
+// stands in.
+uint64_t current_context_id() {
+  static PFN_cuCtxGetCurrent_v4000 get = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f);
+  }();
+  static PFN_cuCtxGetId_v12000 get_id = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuCtxGetId_v12000>(f);
+  }();
+  CUcontext c = nullptr;
+  if (get) get(&c);
+  if (!c) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return uint64_t(1) << 63 | uint64_t(dev);
+  }
+  unsigned long long id = 0;
+  if (get_id && get_id(c, &id) == CUDA_SUCCESS) return uint64_t(id);
+  return uint64_t(reinterpret_cast<uintptr_t>(c));
 }
 
 }  // namespace gbfft
@@ -1201,33 +1238,15 @@ int gbfft_exec_ex(const gbfft_plan* plan, int mode, const void* d_in, void* d_ou
 
 // ---- plan cache -----------------------------------------------------------
 namespace {
-using CacheKey = std::tuple<uintptr_t, int, int64_t, int64_t, int64_t, int64_t, int64_t, int, int, int>;
+using CacheKey = std::tuple<uint64_t, int, int64_t, int64_t, int64_t, int64_t, int64_t, int, int, int>;
 std::mutex g_cache_mu;
 std::map<CacheKey, gbfft_plan*>& cache() {
   static auto* m = new std::map<CacheKey, gbfft_plan*>();
   return *m;
 }
 
-uintptr_t current_context() {
-  static PFN_cuCtxGetCurrent_v4000 fn = [] {
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
-            cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      f = nullptr;
-    return reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f);
-  }();
-  CUcontext c = nullptr;
-  if (fn) fn(&c);
-  if (!c) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    return uintptr_t(0x1000 + dev);
-  }
-  return reinterpret_cast<uintptr_t>(c);
-}
 }  // namespace
+
 
 int gbfft_plan_get(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype,
                    int precision) {
@@ -1236,7 +1255,7 @@ int gbfft_plan_get(gbfft_plan** out, int rank, const int64_t* dims, int kind, in
   cudaFree(nullptr);
   int64_t d[5] = {0, 0, 0, 0, 0};
   for (int i = 0; i < rank; ++i) d[i] = dims[i];
-  CacheKey key{current_context(), rank, d[0], d[1], d[2], d[3], d[4], kind, dtype, precision};
+  CacheKey key{current_context_id(), rank, d[0], d[1], d[2], d[3], d[4], kind, dtype, precision};
   std::lock_guard<std::mutex> lk(g_cache_mu);
   auto it = cache().find(key);
   if (it != cache().end()) {
@@ -1260,7 +1279,8 @@ int gbfft_fft(int mode, int rank, const int64_t* dims, int kind, int dtype, cons
 }
 
 int gbfft_cache_clear(void) {
-  const uintptr_t ctx = current_context();
+  cudaFree(nullptr);
+  const uint64_t ctx = current_context_id();
   std::lock_guard<std::mutex> lk(g_cache_mu);
   for (auto it = cache().begin(); it != cache().end();) {
     if (std::get<0>(it->first) == ctx) {

@@ -99,6 +99,8 @@ void blue_tables(int64_t n, int64_t m, std::vector<cd>& chirp, std::vector<cd>& 
 void host_fft_fp64(std::vector<cd>& x);
 void choose_tile(PassSpec& ps, bool dbl);
 bool fault_injected(const char* what);   // GBFFT_FAULT_INJECT=alloc,...
+// Never-reused identity of the CUDA context current on this thread (plan.cu).
+uint64_t current_context_id();
 bool feature_disabled(const char* what);  // GBFFT_DISABLE=tma,row,cluster (A/B checks)
 
 }  // namespace gbfft

@@ -61,12 +61,17 @@ struct RaggedArgs {
   void* scratch;
   int* counters;  // [0] queue head, [1..] per-(transform, pass) tile counters
   int* status;
+  uint32_t spin_limit;  // bound of one dependency wait (polls)
 };
 
 namespace {
 
 constexpr int kRaggedThreads = 256;
 constexpr uint32_t kDepSpinLimit = 1u << 24;  // ~ seconds with the backoff below
+// GBFFT_FAULT_INJECT=ragged_dep: the plan's first task waits on a counter no
+// task signals, with this short bound (about a millisecond), so the timeout
+// path can be exercised without faulting or hanging anything.
+constexpr uint32_t kInjectedSpinLimit = 1u << 14;
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
   int v;
@@ -127,7 +132,7 @@ __global__ void __launch_bounds__(kRaggedThreads, sizeof(T) == 4 ? 3 : 2) ragged
       if (task.dep >= 0) {
         uint32_t it = 0;
         while (ld_acquire(&a.counters[task.dep]) < task.need) {
-          if (++it > kDepSpinLimit) {
+          if (++it > a.spin_limit) {
             s_timeout = 1;
             atomicExch(a.status, GBFFT_ERR_TIMEOUT_DEVICE);
             break;
@@ -491,6 +496,13 @@ int create_ragged(gbfft_ragged_plan** out, int64_t count, const int64_t* lengths
   }
   // length-1 transforms are the identity for every mode: one grouped copy
   // through a pass-free descriptor is not needed -- they are copied on exec.
+  uint32_t spin_limit = kDepSpinLimit;
+  if (fault_injected("ragged_dep") && !tasks.empty()) {
+    // failure injection: one dependency that nothing ever signals
+    tasks[0].dep = ncounters++;
+    tasks[0].need = 1;
+    spin_limit = kInjectedSpinLimit;
+  }
   p->ntasks = int64_t(tasks.size());
   p->nmembers = int64_t(m_in.size());
   p->ncounters = ncounters;
@@ -558,6 +570,7 @@ int create_ragged(gbfft_ragged_plan** out, int64_t count, const int64_t* lengths
   a.sc_len = p->d_members + 3 * p->nmembers;
   a.scratch = p->d_scratch;
   a.counters = p->d_counters;
+  a.spin_limit = spin_limit;
   a.status = p->d_status;
   if (cudaDeviceSynchronize() != cudaSuccess) return GBFFT_ERR_CUDA;
   *out = p.release();

@@ -14,13 +14,19 @@
 --
 -- What changes relative to the cuFFT module:
 --
---   * withPlan ... cuFFT (PTX.hs:98-124) becomes one unsafe foreign call,
---     gbfft_fft, which looks the plan up in the library's own cache (keyed
---     on the CUDA context and the full shape, not a hash) and enqueues the
---     kernels on the Accelerate stream.  No setStream: the stream is an
---     argument, so concurrent uses of one plan are safe.
---   * Inverse is normalised inside the kernels.  FFT.hs must then skip its
---     own `A.map (/scale)` after a foreign call (see INTEGRATION.md).
+--   * withPlan ... cuFFT (PTX.hs:98-124) becomes two foreign calls.  The
+--     plan lookup, gbfft_plan_get, is imported `safe`: on a cache miss it
+--     builds the plan (and may time candidates with GBFFT_AUTOTUNE=1),
+--     which synchronises the device and can take seconds, so it must not
+--     block the GHC capability.  The cache is the library's own, keyed on
+--     the CUDA context and the full shape rather than a hash.  The launch,
+--     gbfft_exec, only enqueues kernels on the Accelerate stream and is
+--     imported `unsafe`.  No setStream: the stream is an argument, so
+--     concurrent uses of one plan are safe.
+--   * Inverse is normalised inside the kernels, and ranks 4 and 5 of `fft`
+--     run here too.  FFT.hs therefore divides only on the paths that do not
+--     normalise, and its PTX rank guard goes from 3 to 5 (FFT.hs.patch,
+--     next to this module, makes both changes).
 --   * PTX/Plans.hs and the cufft dependency are no longer needed;
 --     PTX/Base.hs (withArray, waypoint) is reused unchanged.
 --
@@ -55,13 +61,21 @@ import Control.Exception
 import Control.Monad.Reader
 import Data.Int
 import Foreign.C.Types
+import Foreign.Marshal.Alloc                                        ( alloca )
 import Foreign.Marshal.Array                                        ( withArrayLen )
+import Foreign.Storable                                             ( peek )
 import Foreign.Ptr
 
 
--- | The entry point: cached plan lookup plus exec (gbfft.h, gbfft_fft).
-foreign import ccall unsafe "gbfft_fft"
-  c_gbfft_fft :: CInt -> CInt -> Ptr Int64 -> CInt -> CInt -> Ptr () -> Ptr () -> Ptr () -> IO CInt
+-- | Cached plan lookup (gbfft.h, gbfft_plan_get): may build and tune a
+-- plan on a miss, so it is a safe call.
+foreign import ccall safe "gbfft_plan_get"
+  c_gbfft_plan_get :: Ptr (Ptr ()) -> CInt -> Ptr Int64 -> CInt -> CInt -> CInt -> IO CInt
+
+-- | Enqueue a plan's kernels on a stream (gbfft.h, gbfft_exec): no host
+-- synchronisation, so an unsafe call.
+foreign import ccall unsafe "gbfft_exec"
+  c_gbfft_exec :: Ptr () -> CInt -> Ptr () -> Ptr () -> Ptr () -> IO CInt
 
 foreign import ccall unsafe "gbfft_error_string"
   c_gbfft_error_string :: CInt -> IO (Ptr CChar)
@@ -149,8 +163,15 @@ fft' kind mode shR eR =
 gbfft :: CInt -> Mode -> NumericR e -> [Int64] -> Stream -> DevicePtr e -> DevicePtr e -> IO ()
 gbfft kind mode eR dims stream d_in d_out =
   withLifetime stream $ \s ->
-  withArrayLen dims   $ \rank pdims -> do
-    r <- c_gbfft_fft (modeCode mode) (fromIntegral rank) pdims kind (dtypeCode eR)
-                     (castPtr (useDevicePtr d_in)) (castPtr (useDevicePtr d_out))
-                     (castPtr (CUDA.useStream s))
+  withArrayLen dims   $ \rank pdims ->
+  alloca              $ \pplan -> do
+    r0 <- c_gbfft_plan_get pplan (fromIntegral rank) pdims kind (dtypeCode eR) precisionPlain
+    when (r0 /= 0) $ throwIO (GbfftException (fromIntegral r0))
+    plan <- peek pplan
+    r <- c_gbfft_exec plan (modeCode mode) (castPtr (useDevicePtr d_in)) (castPtr (useDevicePtr d_out))
+                      (castPtr (CUDA.useStream s))
     when (r /= 0) $ throwIO (GbfftException (fromIntegral r))
+
+-- GBFFT_PLAIN: FP32 for Complex Float, FP64 for Complex Double
+precisionPlain :: CInt
+precisionPlain = 0

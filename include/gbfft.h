@@ -247,17 +247,20 @@ int gbfft_specconv_plan_destroy(gbfft_specconv_plan* plan);
 
 /* ---- allocation-free transform ------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot
- * allocate device memory -- a host that owns the device heap (Accelerate's
- * PTX backend passes arrays from its own allocator) or code recording a CUDA
- * graph by stream capture, where cudaMalloc is not allowed.  Transforms
- * `batch` contiguous rows of length n (Bluestein's algorithm, four passes,
- * any n) with Mode semantics as gbfft_exec (Inverse divides by n), reading
- * d_in and writing d_out, and allocates nothing: its tables and padded work
- * sequences live in one fixed 16 MiB __device__ array per device, kept until
- * the process exits.  The first call on a device sets that array up (make it
- * before any stream capture).  Calls share the array, so calls that overlap
- * on the GPU race.  Requests whose tables plus 2 * batch * m elements (m, the
- * padded length, is about 2n to 4n) exceed 16 MiB return GBFFT_ERR_TOO_LARGE. */
+ * allocate device memory, such as a host that owns the device heap itself
+ * (Accelerate's PTX backend passes arrays from its own allocator and keeps
+ * its own account of device memory).  Transforms `batch` contiguous rows of
+ * length n (Bluestein's algorithm, four passes, any n) with Mode semantics
+ * as gbfft_exec (Inverse divides by n), reading d_in and writing d_out, and
+ * allocates nothing: its tables and padded work sequences live in one fixed
+ * 16 MiB __device__ array per device (per CUDA context), kept until the
+ * process exits.  Each call resolves the array's address in the context
+ * current on the calling thread; the first call in a context also sets the
+ * kernels up and uploads the tables (make it before any stream capture).
+ * Calls share the array and it keeps the last call's tables, so calls that
+ * overlap on the GPU race.  Requests whose tables plus 2 * batch * m
+ * elements (m, the padded length, is about 2n to 4n) exceed 16 MiB return
+ * GBFFT_ERR_TOO_LARGE. */
 int gbfft_fft_noalloc(int mode, int64_t n, int64_t batch, int dtype, const void* d_in, void* d_out,
                       void* stream);
 

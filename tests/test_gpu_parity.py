@@ -372,15 +372,28 @@ def test_row_kernel_input_not_16_byte_aligned(gbfft_lib):
 
 
 # ---- split-FP16 tensor-core radix-16 stages ---------------------------------
+TC_KERNELS = ("rowfft_tc_kernel",)
+
+
+def test_split_fp16_without_tensor_core_pass_is_refused(gbfft_lib):
+    # a split-FP16 request that no tensor-core kernel serves is refused, not
+    # silently run in FP32
+    g = gbfft_lib
+    from gbfft import _lib as L
+    with pytest.raises(L.GbfftError) as ei:
+        g.Plan((4, 96), kind="many", dtype=torch.complex64, precision="split_fp16")
+    assert ei.value.status == L.ERR_UNSUPPORTED
 @pytest.mark.parametrize("shape,kind", [((4096, 4096), "full"), ((300, 4096), "many"), ((100, 1024), "many"),
                                         ((64, 256), "many"), ((8, 8192), "many"), ((17, 2048), "many"),
-                                        ((5, 512), "many"), ((3, 256, 256), "full"), ((6, 1000), "many")])
+                                        ((5, 512), "many"), ((3, 256, 256), "full")])
 def test_split_fp16_accuracy(gbfft_lib, shape, kind):
     # the specification's bar: <= 2e-6 relative L2 against FP64
     g = gbfft_lib
     rng = np.random.default_rng(sum(shape))
     x = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
     plan = g.Plan(shape, kind=kind, dtype=torch.complex64, precision="split_fp16")
+    # a split-FP16 plan runs at least one pass on the tensor cores
+    assert any(k in TC_KERNELS for k in plan.pass_kernels()), (shape, plan.pass_kernels())
     xt = torch.from_numpy(x).cuda()
     fam = {2: "fft2D", 3: "fft3D"}[len(shape)] if kind == "full" else "fft"
     for mode in MODES:

@@ -55,6 +55,41 @@ def test_ragged_small_mixed(gbfft_lib):
     assert torch.equal(xt.cpu(), torch.from_numpy(x))
 
 
+def test_ragged_dependency_wait_times_out(gbfft_lib, monkeypatch):
+    """A device-side wait that runs out: GBFFT_FAULT_INJECT=ragged_dep makes the
+    plan's first task wait on a counter that no task ever signals, with a
+    short bound.  The launch must end by itself, report GBFFT_ERR_TIMEOUT
+    through gbfft_ragged_status, and leave the GPU usable: a normal plan
+    afterwards is correct and reports OK."""
+    import time
+    g = gbfft_lib
+    from gbfft import _lib as L
+    lengths = np.array([16, 1000, 1009, 4096, 8192, 65521, 300, 7], np.int64)
+    modes = np.array([-1, 1, 2, -1, 2, -1, 1, 2], np.int32)
+    rng = np.random.default_rng(5)
+    total = int(lengths.sum())
+    x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex64)
+    xt = torch.from_numpy(x).cuda()
+    monkeypatch.setenv("GBFFT_FAULT_INJECT", "ragged_dep")
+    bad = g.RaggedPlan(lengths, modes)
+    monkeypatch.delenv("GBFFT_FAULT_INJECT")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bad(xt)
+    st = bad.status()  # synchronises the stream
+    dt = time.perf_counter() - t0
+    assert st == L.ERR_TIMEOUT
+    assert dt < 5.0, dt
+    assert bad.status() == L.OK  # the status word was cleared by the read
+    bad.close()
+    good = g.RaggedPlan(lengths, modes)
+    y = good(xt)
+    torch.cuda.synchronize()
+    assert good.status() == L.OK
+    check_segments(lengths, modes, good.offsets, x, y.cpu().numpy())
+    good.close()
+
+
 def test_ragged_offsets_with_gaps_and_double(gbfft_lib):
     g = gbfft_lib
     lengths = np.array([16, 1000, 1009, 5, 8192, 3], np.int64)
