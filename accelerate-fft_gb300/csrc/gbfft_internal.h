@@ -19,6 +19,8 @@ constexpr int GBFFT_ERR_INTERNAL_DEVICE = 7;
 // Largest transform length one CTA computes in shared memory (two ping-pong
 // buffers of one column each); longer axes are split four-step.
 constexpr int kCapC32 = 8192;
+// Longest row the split-FP16 dense-DFT kernels take (folded length 1025).
+constexpr int kTcDftMaxN = 2048;
 constexpr int kCapC64 = 4096;
 
 // Pre- and post-operations fused into a pencil pass.
@@ -47,6 +49,9 @@ enum KernelId : int {
   K_COL4096 = 2,  // 8-CTA cluster kernel for stride-S axes of length 4096
   K_ROW_TC = 3,   // contiguous rows, radix-16 stages as split-FP16 tensor-core GEMMs
   K_STRIDED = 4,  // register-resident strided pencils, W adjacent columns per CTA
+  K_TC_FOLD = 5,  // split-FP16 dense DFT, step 1: fold rows into hi/lo FP16 operand tiles
+  K_TC_DFT = 6,   // split-FP16 dense DFT, step 2: tcgen05 GEMM against cos/sin tiles
+  K_TC_DFT8 = 7,  // split-FP16 rows n = 8 * n2: radix-8 on the CUDA cores, dense n2 stage on tcgen05
 };
 
 struct StageInfo {
@@ -101,6 +106,9 @@ struct PassDesc {
   // element with axis index l = k*lout_es + c*lout_cs is stored
   // (rot(l) - l) * rot_stride elements away, rot(l) = (l - rot_s) mod rot_n
   int64_t rot_n, rot_s, rot_stride;
+  // K_TC_FOLD / K_TC_DFT: folded length P (= floor(n/2) + 1), K chunks of
+  // 32 and output chunks of 128 frequencies covering it
+  int tc_p, tc_kc, tc_nc;
 };
 
 // Address offset of F_ROT_OUT for axis index l (0 without the flag).
@@ -138,6 +146,8 @@ cudaError_t launch_str(const PassDesc& d, bool dbl, cudaStream_t s);
 cudaError_t prepare_row_tc_kernels();
 cudaError_t launch_row_tc(const PassDesc& d, cudaStream_t s);
 cudaError_t launch_col4096(const PassDesc& d, bool dbl, cudaStream_t s);
+cudaError_t prepare_tcdft_kernels();
+cudaError_t launch_tcdft(const PassDesc& d, cudaStream_t s);
 int col_tile_width(int variant);
 
 }  // namespace gbfft

@@ -920,14 +920,69 @@ int build_plan(gbfft_plan* p, bool dry) {
   return GBFFT_OK;
 }
 
-// Split-FP16 plans: the FP32 plan with every contiguous-row pass whose
-// length has radix-16 stages moved to the tensor-core kernel.  D is the
-// 32 x 32 real form of the forward DFT-16 (rows: Re y_n then Im y_n;
-// columns: Re x_k then Im x_k), split as D_hi + D_lo in FP16.
+// Split-FP16 dense rows: the innermost axis of length w (one FP32 pass from
+// the input to the output, no plan scratch) becomes the fold pass and the
+// tensor-core product pass of tcdft.cu, for lengths without a radix-16
+// tensor-core row kernel.  Returns GBFFT_ERR_UNSUPPORTED when the plan does
+// not have that shape (the caller then tries the radix-16 form).
+static int build_split_dense(gbfft_plan* p) {
+  const int64_t w = p->dims[p->rank - 1];
+  if (p->passes.empty() || !tcdft_available(w) || row_tc_available(int(w)) || p->d_scratch)
+    return GBFFT_ERR_UNSUPPORTED;
+  const PassSpec first = p->passes[0];
+  if (first.src != R_IN || first.dst != R_OUT || !first.axis_final) return GBFFT_ERR_UNSUPPORTED;
+  const int64_t rows = p->total / w;
+  Builder B;
+  std::vector<PassSpec> tc;
+  const bool fused = tcdft8_available(w);  // n = 8 * odd: one pass, no scratch
+  int st = fused ? tcdft8_add_pass(B, w, rows, w, w, R_IN, R_OUT, tc)
+                 : tcdft_add_passes(B, w, rows, w, w, R_IN, R_OUT, tc);
+  if (st != GBFFT_OK) return st;
+  if (fault_injected("alloc")) return GBFFT_ERR_ALLOC;
+  if (cudaMalloc(&p->d_tcmat, B.blob.size()) != cudaSuccess) return GBFFT_ERR_ALLOC;
+  if (cudaMemcpy(p->d_tcmat, B.blob.data(), B.blob.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return GBFFT_ERR_CUDA;
+  if (!fused) {
+    p->scratch_bytes = tcdft_scratch_bytes(w, rows);
+    if (cudaMalloc(&p->d_scratch, p->scratch_bytes) != cudaSuccess) return GBFFT_ERR_ALLOC;
+    if (cudaEventCreateWithFlags(&p->scratch_ev, cudaEventDisableTiming) != cudaSuccess) return GBFFT_ERR_CUDA;
+  }
+  for (PassSpec& ps : tc) {
+    ps.d.status = first.d.status;
+    if (ps.tw_off >= 0) ps.d.tw = static_cast<unsigned char*>(p->d_tcmat) + ps.tw_off;
+  }
+  std::vector<PassSpec> passes = tc;
+  passes.insert(passes.end(), p->passes.begin() + 1, p->passes.end());
+  p->passes = passes;
+  const size_t cut = p->desc.find('[');
+  const size_t end = p->desc.find(']');
+  char buf[160];
+  if (fused)
+    std::snprintf(buf, sizeof buf, "[n=%lld = 8x%d: radix-8 + tcgen05 split-fp16 dense %d (P=%d)]", (long long)w,
+                  tc[0].d.tc_nc, tc[0].d.tc_nc, tc[0].d.tc_p);
+  else
+    std::snprintf(buf, sizeof buf, "[n=%lld tensor-core dense DFT: fold + tcgen05 split-fp16 (P=%d, %dx%d chunks)]",
+                  (long long)w, tc[0].d.tc_p, tc[0].d.tc_kc, tc[0].d.tc_nc);
+  if (cut != std::string::npos && end != std::string::npos && end > cut)
+    p->desc = p->desc.substr(0, cut) + buf + p->desc.substr(end + 1);
+  else
+    p->desc += buf;
+  p->desc += " split-fp16(tensor-core dense rows)";
+  return GBFFT_OK;
+}
+
+// Split-FP16 plans: the FP32 plan with its contiguous-row passes moved to the
+// tensor cores -- lengths with radix-16 stages to the radix-16 tensor-core
+// row kernel, other row lengths up to kTcDftMaxN to the dense DFT
+// (build_split_dense).  For the radix-16 kernel D is the 32 x 32 real form of
+// the forward DFT-16 (rows: Re y_n then Im y_n; columns: Re x_k then Im x_k),
+// split as D_hi + D_lo in FP16.
 int build_split_plan(gbfft_plan* p) {
   if (p->dbl) return GBFFT_ERR_INVALID_ARG;
   int st = build_plan(p, false);
   if (st != GBFFT_OK) return st;
+  st = build_split_dense(p);
+  if (st != GBFFT_ERR_UNSUPPORTED) return st;
   std::vector<__half> dm(2048);
   for (int n = 0; n < 32; ++n)
     for (int k = 0; k < 32; ++k) {

@@ -162,6 +162,14 @@ int build_split_plan(gbfft_plan* p);
 int create_plan(gbfft_plan** out, int rank, const int64_t* dims, int kind, int dtype, int precision,
                 const TuneChoice* forced);
 int build_split_plan(gbfft_plan* p);
+// split-FP16 dense DFT of contiguous rows (tcdft.cu)
+bool tcdft_available(int64_t n);
+size_t tcdft_scratch_bytes(int64_t n, int64_t rows);
+int tcdft_add_passes(Builder& B, int64_t n, int64_t rows, int64_t in_cs, int64_t out_cs, int src, int dst,
+                     std::vector<PassSpec>& passes);
+bool tcdft8_available(int64_t n);
+int tcdft8_add_pass(Builder& B, int64_t n, int64_t rows, int64_t in_cs, int64_t out_cs, int src, int dst,
+                    std::vector<PassSpec>& passes);
 int exec_passes(const gbfft_plan* p, const std::vector<PassSpec>& passes, int mode, double inv_norm,
                 const void* in, void* out, cudaStream_t s, int opts = 0, bool centre_fused = false);
 }  // namespace gbfft

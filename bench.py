@@ -157,6 +157,10 @@ WORKLOADS = {
 }
 
 
+for _name, _wl in WORKLOADS.items():
+    _wl["name"] = _name
+
+
 # DRAM bytes (read + write) per launch of a workload's dominant kernel from one
 # ncu capture (profiles/<kernel>_<workload>.md).  Under ncu's serialised
 # replay part of a launch's writes is still in L2 when it ends, so these read
@@ -268,6 +272,32 @@ def run_reference(args, wl):
 
 
 def run_gbfft(args, wl):
+    line = measure_gbfft(args, wl)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    finish_dist()
+
+
+def finish_dist():
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        import torch.distributed as dist
+        if dist.is_initialized():
+            dist.destroy_process_group()
+
+
+def init_dist(local):
+    import torch
+    torch.cuda.set_device(local)
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("nccl")
+
+
+def measure_gbfft(args, wl, headline=True):
+    """One plan workload (fft / fft1D / fft2D / fft3D): the JSON line's fields
+    on rank 0, None on the other ranks.  headline=False skips the access-pattern
+    probe (reported for the headline workload only)."""
     import numpy as np
     import torch
 
@@ -275,11 +305,8 @@ def run_gbfft(args, wl):
     from gbfft import _lib as L
 
     world, rank, local = dist_init()
-    torch.cuda.set_device(local)
+    init_dist(local)
     dev = torch.device("cuda", local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
     lib = L.lib()
     shape = wl["shape"]
     dtype = torch.complex128 if wl["dtype"] == "c64" else torch.complex64
@@ -361,7 +388,7 @@ def run_gbfft(args, wl):
     ceiling = None
     full2 = wl["kind"] == "full" and len(shape) >= 2
     rowsv = wl["kind"] == "many" and len(shape) >= 2 and shape[-1] % 2 == 0
-    if rank == 0 and (full2 or rowsv) and elem == 8 and nlaunch:
+    if rank == 0 and headline and (full2 or rowsv) and elem == 8 and nlaunch:
         rows, cols = (shape[0], nelem // shape[0]) if full2 else (nelem // shape[-1], shape[-1])
         gbs = {}
         for w in ((16, cols) if full2 else (cols,)):
@@ -532,7 +559,7 @@ def run_gbfft(args, wl):
                        "autotune": tune_report.strip().splitlines()[-1] if tune_report else "off"},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                          "frac": ach / peak,
-                         "traffic": ncu_traffic(args.workload, kernels[dom] if npass else None),
+                         "traffic": ncu_traffic(wl["name"], kernels[dom] if npass else None),
                          "peak_source": peak_kind,
                          "kernel": "pass %d of %d (%s)" % (dom, npass, kernels[dom] if npass else "-"),
                          "bytes_alg_per_launch": bytes_pass,
@@ -553,12 +580,20 @@ def run_gbfft(args, wl):
             "cufft_comparator_ms": cufft_ms,
             "cpu_baseline": cpu,
         }
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+        plan.close()
+        return line
+    plan.close()
+    return None
 
 
 def run_ragged(args, wl):
+    line = measure_ragged(args, wl)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    finish_dist()
+
+
+def measure_ragged(args, wl, cpu_budget_s=12.0):
     import numpy as np
     import torch
 
@@ -567,11 +602,8 @@ def run_ragged(args, wl):
     from gbfft import synth
 
     world, rank, local = dist_init()
-    torch.cuda.set_device(local)
+    init_dist(local)
     dev = torch.device("cuda", local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
     lengths, modes = synth.ragged_lengths(wl["count"], seed=4)
     total = int(lengths.sum())
     g = torch.Generator().manual_seed(1234 + rank)
@@ -649,7 +681,7 @@ def run_ragged(args, wl):
             e2e.append(a.elapsed_time(b))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline_ragged(lengths, modes, plan.offsets, x_cpu.numpy())
+        cpu = cpu_baseline_ragged(lengths, modes, plan.offsets, x_cpu.numpy(), budget_s=cpu_budget_s)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
@@ -662,7 +694,7 @@ def run_ragged(args, wl):
                        "autotune": tune_report.strip().splitlines()[-1] if tune_report else "off",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                         "frac": ach / peak, "traffic": ncu_traffic(args.workload, "ragged_kernel"),
+                         "frac": ach / peak, "traffic": ncu_traffic(wl["name"], "ragged_kernel"),
                          "peak_source": peak_kind,
                          "kernel": "ragged_kernel<float> (the single persistent launch)",
                          "bytes_alg_per_launch": bytes_alg, "kernel_ms": ms},
@@ -675,48 +707,54 @@ def run_ragged(args, wl):
                     "ms_per_step": statistics.mean(e2e)},
             "gpu_launches": args.steps, "clocks": clocks, "cpu_baseline": cpu,
         }
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+        plan.close()
+        return line
+    plan.close()
+    return None
 
 
-def grf_fields(shape, seed):
-    """Gaussian random fields with power spectrum ~ |k|^-5/3: white noise
-    shaped in Fourier space (numpy FP64 on the host), normalised to unit
-    variance per component."""
-    import numpy as np
+def grf_fields(shape, seed, device="cpu"):
+    """Gaussian random fields with power spectrum ~ |k|^-5/3: seeded white
+    noise shaped in Fourier space, normalised to unit variance per component.
+    Input synthesis only (torch's FFT on `device`), not the measured path."""
+    import torch
     b, d, h, w = shape
-    rng = np.random.default_rng(seed)
-    kz = np.fft.fftfreq(d)[:, None, None]
-    ky = np.fft.fftfreq(h)[None, :, None]
-    kx = np.fft.fftfreq(w)[None, None, :]
-    k = np.sqrt(kx * kx + ky * ky + kz * kz)
+    g = torch.Generator(device=device).manual_seed(seed)
+    kz = torch.fft.fftfreq(d, device=device, dtype=torch.float64)[:, None, None]
+    ky = torch.fft.fftfreq(h, device=device, dtype=torch.float64)[None, :, None]
+    kx = torch.fft.fftfreq(w, device=device, dtype=torch.float64)[None, None, :]
+    k = torch.sqrt(kx * kx + ky * ky + kz * kz)
     k[0, 0, 0] = 1.0
     amp = (k ** (-5.0 / 3.0)) ** 0.5
     amp[0, 0, 0] = 0.0
-    out = np.empty(shape, np.complex64)
+    out = torch.empty(shape, dtype=torch.complex64, device=device)
     for i in range(b):
-        noise = rng.standard_normal((d, h, w)) + 1j * rng.standard_normal((d, h, w))
-        f = np.fft.ifftn(np.fft.fftn(noise) * amp)
-        f /= np.sqrt(np.mean(np.abs(f) ** 2) / 2)
-        out[i] = f.astype(np.complex64)
+        noise = torch.complex(torch.randn((d, h, w), generator=g, device=device, dtype=torch.float64),
+                              torch.randn((d, h, w), generator=g, device=device, dtype=torch.float64))
+        f = torch.fft.ifftn(torch.fft.fftn(noise) * amp)
+        f = f / torch.sqrt(torch.mean(torch.abs(f) ** 2) / 2)
+        out[i] = f.to(torch.complex64)
     return out
 
 
 def run_specconv(args, wl):
+    line = measure_specconv(args, wl)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    finish_dist()
+
+
+def measure_specconv(args, wl):
     import numpy as np
     import torch
 
     import gbfft
 
     world, rank, local = dist_init()
-    torch.cuda.set_device(local)
+    init_dist(local)
     dev = torch.device("cuda", local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
     shape = wl["shape"]
-    x_cpu = torch.from_numpy(grf_fields(shape, 5 + rank))
+    x_cpu = grf_fields(shape, 5 + rank, device=dev).cpu()
     g = np.random.default_rng(55)
     H_cpu = torch.from_numpy(((g.standard_normal(shape[1:]) + 1j * g.standard_normal(shape[1:]))
                               / np.sqrt(2)).astype(np.complex64))
@@ -800,11 +838,38 @@ def run_specconv(args, wl):
             "e2e": {"value": fl * world / (statistics.mean(e2e) * 1e-3) / 1e9, "unit": "GFLOP/s",
                     "h2d_bytes_per_step": x.numel() * 8, "d2h_bytes_per_step": x.numel() * 8,
                     "ms_per_step": statistics.mean(e2e)},
-            "gpu_launches": args.steps * 12, "clocks": clocks, "cpu_baseline": None,
+            "gpu_launches": args.steps * 12, "clocks": clocks,
+            "cpu_baseline": (cpu_baseline_specconv(x_cpu.numpy(), H_cpu.numpy(), fl / shape[0])
+                             if world == 1 and not args.no_cpu else None),
         }
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+        plan.close()
+        return line
+    plan.close()
+    return None
+
+
+def cpu_baseline_specconv(x_np, H_np, flops_per_field):
+    """The reference's composition of the spectral convolution and its
+    gradient (fft3D Forward, product, fft3D Inverse; the adjoint as three more
+    fft3D calls and two products) through the oracle's restatement of fft3D,
+    on the host cores, for a bounded sample: one of the fields."""
+    import numpy as np
+    from oracle import lib as O
+    threads = os.cpu_count() or 1
+    x = x_np[0]
+    t0 = time.perf_counter()
+    X = O.fft3D(0, x, threads=threads)                      # Forward
+    y = O.fft3D(2, X * H_np, threads=threads)               # Inverse (y; also g_y for L = 1/2|y|^2)
+    gY = O.fft3D(0, y, threads=threads) / np.float32(y.size)  # g_Y = Forward(g_y) / N
+    Xr = O.fft3D(0, x, threads=threads)                     # X recomputed, as the adjoint kernel does
+    gH = np.conj(Xr) * gY                                   # this field's share of g_H
+    gx = O.fft3D(1, np.conj(H_np) * gY, threads=threads)    # Reverse
+    dt = time.perf_counter() - t0
+    del gH, gx
+    return {"value": flops_per_field / dt / 1e9, "unit": "GFLOP/s", "cores": threads, "kind": "port",
+            "sample": "1 of the 8 fields: forward (2 fft3D) and adjoint (3 fft3D) composed from the oracle "
+                      "C++ restatement of fft3D (FFT.hs:150-187) and elementwise products",
+            "seconds": dt}
 
 
 def cpu_baseline_ragged(lengths, modes, offsets, x_np, budget_s=12.0):
@@ -837,13 +902,121 @@ def cpu_baseline_ragged(lengths, modes, offsets, x_np, budget_s=12.0):
                       "one transform per host thread" % (done_n, len(lengths))}
 
 
+def _compact(line):
+    """The per-config summary carried in the headline line."""
+    if line is None:
+        return None
+    keep = {}
+    for k in ("ms_per_step", "value", "unit", "rel_err_vs_fp64", "roundtrip_rel_err", "cufft_comparator_ms",
+              "cpu_baseline", "clocks", "gpu_launches"):
+        if k in line:
+            keep[k] = line[k]
+    keep["workload"] = line["config"]["workload"]
+    if "plan" in line["config"]:
+        keep["plan"] = line["config"]["plan"]
+    r = line.get("roofline", {})
+    keep["roofline"] = {k: r.get(k) for k in ("bound", "achieved", "peak", "unit", "frac", "traffic", "kernel",
+                                              "kernel_ms", "bytes_alg_per_launch") if k in r}
+    if "roofline_transform" in line:
+        keep["roofline_transform"] = {k: line["roofline_transform"][k] for k in ("achieved", "frac", "kernels")}
+    e = line.get("e2e") or {}
+    keep["e2e"] = {k: e.get(k) for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step",
+                                         "ms_per_step")}
+    if line.get("other_precision"):
+        keep["other_precision"] = line["other_precision"]
+    return keep
+
+
+def measure_config3(args):
+    """Config 3: fft (innermost axis) over a 65536 x 1000 and a 4096 x 1009
+    Complex Float array, plain FP32 and split-FP16 tensor-core plans; the
+    workload's time is the sum of the two transforms."""
+    a = measure_gbfft(args, WORKLOADS["many_65536x1000"], headline=False)
+    b = measure_gbfft(args, WORKLOADS["many_4096x1009"], headline=False)
+    if a is None or b is None:
+        return None
+    peak, _ = load_peaks()
+    shapes = [(65536, 1000), (4096, 1009)]
+    fl = [flops_of(sh, "many") for sh in shapes]
+    byts = sum(2.0 * 8 * sh[0] * sh[1] for sh in shapes)
+    ms = a["ms_per_step"] + b["ms_per_step"]
+    out = {"workload": "fft innermost axis, Complex Float 65536x1000 (2^3*5^3) plus 4096x1009 (prime), N(0,1)",
+           "ms_per_step": ms, "value": sum(fl) / (ms * 1e-3) / 1e9, "unit": "GFLOP/s",
+           "rel_err_vs_fp64": max(a["rel_err_vs_fp64"] or 0, b["rel_err_vs_fp64"] or 0),
+           "roofline": {"bound": "hbm", "achieved": byts / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": byts / (ms * 1e-3) / 1e9 / peak, "bytes_alg": byts}}
+    oa, ob = a.get("other_precision") or {}, b.get("other_precision") or {}
+    if "ms_per_step" in oa and "ms_per_step" in ob:
+        ms2 = oa["ms_per_step"] + ob["ms_per_step"]
+        out["split_fp16"] = {"ms_per_step": ms2, "value": sum(fl) / (ms2 * 1e-3) / 1e9, "unit": "GFLOP/s",
+                             "roofline_frac": byts / (ms2 * 1e-3) / 1e9 / peak,
+                             "rel_err_vs_fp64": max(oa.get("rel_err_vs_fp64") or 0, ob.get("rel_err_vs_fp64") or 0),
+                             "speedup_of_split_fp16_over_fp32": ms / ms2,
+                             "kernels": {"65536x1000": oa.get("kernels"), "4096x1009": ob.get("kernels")}}
+    else:
+        out["split_fp16"] = {"unavailable": [oa.get("unavailable"), ob.get("unavailable")]}
+    ea, eb = a["e2e"], b["e2e"]
+    ems = ea["ms_per_step"] + eb["ms_per_step"]
+    out["e2e"] = {"value": sum(fl) / (ems * 1e-3) / 1e9, "unit": "GFLOP/s",
+                  "h2d_bytes_per_step": ea["h2d_bytes_per_step"] + eb["h2d_bytes_per_step"],
+                  "d2h_bytes_per_step": ea["d2h_bytes_per_step"] + eb["d2h_bytes_per_step"], "ms_per_step": ems}
+    ca, cb = a.get("cpu_baseline"), b.get("cpu_baseline")
+    if ca and cb:
+        t = fl[0] / (ca["value"] * 1e9) + fl[1] / (cb["value"] * 1e9)
+        out["cpu_baseline"] = {"value": sum(fl) / t / 1e9, "unit": "GFLOP/s", "cores": ca["cores"], "kind": "port",
+                               "sample": "%s; %s" % (ca["sample"], cb["sample"])}
+    if a.get("cufft_comparator_ms") and b.get("cufft_comparator_ms"):
+        out["cufft_comparator_ms"] = a["cufft_comparator_ms"] + b["cufft_comparator_ms"]
+    out["arrays"] = {"65536x1000": _compact(a), "4096x1009": _compact(b)}
+    return out
+
+
+def run_all(args):
+    """The default run: config 2 (fft2D 4096^2, the headline `value`) with
+    configs 1, 3, 4 and 5 measured in the same process and reported under
+    `configs`."""
+    import copy
+    head = measure_gbfft(args, WORKLOADS["fft2d_4096"])
+    sub = copy.copy(args)
+    sub.steps = max(3, min(args.steps, 10))
+    sub.warmup = 3
+    c1 = measure_gbfft(sub, WORKLOADS["fft1d_1024_c64"], headline=False)
+    c3 = measure_config3(sub)
+    subr = copy.copy(sub)
+    subr.no_tune = True  # the ragged tuner keeps the defaults for this batch (measured); plan creation stays short
+    c4 = measure_ragged(subr, WORKLOADS["ragged_20000"], cpu_budget_s=8.0)
+    c5 = measure_specconv(sub, WORKLOADS["specconv_8x256"])
+    if head is not None:
+        c4c = _compact(c4)
+        if c4 is not None:
+            c4c["per_transform_comparator"] = c4.get("per_transform_comparator")
+            c4c["rel_err_vs_fp64_max_of_200"] = c4.get("rel_err_vs_fp64_max_of_200")
+            c4c["device_status"] = c4.get("device_status")
+            pt = (c4.get("per_transform_comparator") or {}).get("ms_per_step")
+            c4c["speedup_over_one_launch_per_transform"] = pt / c4["ms_per_step"] if pt else None
+        c5c = _compact(c5)
+        if c5 is not None:
+            c5c["fwd_ms"] = c5["roofline"]["fwd_ms"]
+            c5c["adjoint_ms"] = c5["roofline"]["bwd_ms"]
+        head["configs"] = {
+            "1": _compact(c1),
+            "2": {"workload": head["config"]["workload"], "see": "the headline fields of this line"},
+            "3": c3, "4": c4c, "5": c5c,
+            "note": "configs 1, 3, 4, 5 timed as the headline (CUDA events, L2 flushed between steps) with "
+                    "%d steps after 3 warm-up steps each" % sub.steps,
+        }
+        print(json.dumps(head), flush=True)
+    finish_dist()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbfft", choices=["gbfft", "reference"])
-    ap.add_argument("--workload", default="fft2d_4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="all", choices=["all"] + sorted(WORKLOADS),
+                    help="all (default): config 2 as the headline plus configs 1, 3, 4, 5 under `configs`")
     ap.add_argument("--precision", default="plain", choices=["plain", "split_fp16"])
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cufft", action="store_true")
@@ -856,10 +1029,14 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    wl = WORKLOADS[args.workload]
     if args.impl == "reference":
-        run_reference(args, wl)
-    elif wl["kind"] == "ragged":
+        run_reference(args, WORKLOADS["fft2d_4096" if args.workload == "all" else args.workload])
+        return
+    if args.workload == "all":
+        run_all(args)
+        return
+    wl = WORKLOADS[args.workload]
+    if wl["kind"] == "ragged":
         run_ragged(args, wl)
     elif wl["kind"] == "specconv":
         run_specconv(args, wl)

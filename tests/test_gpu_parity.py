@@ -372,7 +372,7 @@ def test_row_kernel_input_not_16_byte_aligned(gbfft_lib):
 
 
 # ---- split-FP16 tensor-core radix-16 stages ---------------------------------
-TC_KERNELS = ("rowfft_tc_kernel",)
+TC_KERNELS = ("rowfft_tc_kernel", "tcdft_mma_kernel", "tcdft8_kernel")
 
 
 def test_split_fp16_without_tensor_core_pass_is_refused(gbfft_lib):
@@ -381,11 +381,21 @@ def test_split_fp16_without_tensor_core_pass_is_refused(gbfft_lib):
     g = gbfft_lib
     from gbfft import _lib as L
     with pytest.raises(L.GbfftError) as ei:
-        g.Plan((4, 96), kind="many", dtype=torch.complex64, precision="split_fp16")
+        g.Plan((4, 3000), kind="many", dtype=torch.complex64, precision="split_fp16")
     assert ei.value.status == L.ERR_UNSUPPORTED
+
+
 @pytest.mark.parametrize("shape,kind", [((4096, 4096), "full"), ((300, 4096), "many"), ((100, 1024), "many"),
                                         ((64, 256), "many"), ((8, 8192), "many"), ((17, 2048), "many"),
-                                        ((5, 512), "many"), ((3, 256, 256), "full")])
+                                        ((5, 512), "many"), ((3, 256, 256), "full"),
+                                        # dense tensor-core rows (tcdft): Bluestein-class and other lengths
+                                        ((4096, 1009), "many"), ((130, 1009), "many"), ((1009,), "full"),
+                                        ((3, 7, 97), "many"), ((257, 3), "many"), ((9, 4), "many"),
+                                        ((6, 1000), "many"), ((40, 2047), "many"), ((5, 2048 - 2), "many"),
+                                        ((20, 1009), "full"),
+                                        # fused radix-8 + dense odd stage (tcdft8): n = 8 * odd
+                                        ((8192, 1000), "many"), ((33, 1000), "many"), ((17, 24), "many"),
+                                        ((5, 3, 40), "many"), ((100, 1016), "many"), ((31, 504), "many")])
 def test_split_fp16_accuracy(gbfft_lib, shape, kind):
     # the specification's bar: <= 2e-6 relative L2 against FP64
     g = gbfft_lib
@@ -395,7 +405,7 @@ def test_split_fp16_accuracy(gbfft_lib, shape, kind):
     # a split-FP16 plan runs at least one pass on the tensor cores
     assert any(k in TC_KERNELS for k in plan.pass_kernels()), (shape, plan.pass_kernels())
     xt = torch.from_numpy(x).cuda()
-    fam = {2: "fft2D", 3: "fft3D"}[len(shape)] if kind == "full" else "fft"
+    fam = {1: "fft1D", 2: "fft2D", 3: "fft3D"}[len(shape)] if kind == "full" else "fft"
     for mode in MODES:
         y = plan(mode, xt).cpu().numpy()
         e = rel_l2(y, np_reference(fam, MODE_IDX[mode], x))
