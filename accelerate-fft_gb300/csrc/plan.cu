@@ -881,6 +881,14 @@ int build_plan(gbfft_plan* p, bool dry) {
       p->passes[i].d.flags |= F_L2_IN_FIRST;
     }
   }
+  // double-buffered register rows store their outputs evict_last for the
+  // next pass (fft2D 4096^2 column pass 86 -> 84 us); GBFFT_L2_KEEP=k keeps
+  // only the first k elements of each row
+  for (PassSpec& ps : p->passes)
+    if (ps.d.kernel == K_ROW) ps.d.l2_keep = ps.d.n;
+  if (const char* kp = std::getenv("GBFFT_L2_KEEP"))
+    for (PassSpec& ps : p->passes)
+      if (ps.d.kernel == K_ROW) ps.d.l2_keep = std::atoll(kp);
   unsigned char* base = static_cast<unsigned char*>(p->d_tables);
   p->d_status = reinterpret_cast<int*>(base + status_off);
   const bool tma = !feature_disabled("tma");

@@ -19,23 +19,30 @@
 //
 // Precision: every operand is split in FP16 as v = hi + lo (each row scaled by
 // a power of two that puts its largest component in [2^12, 2^13), so every
-// folded value stays below 2^14), the three
-// products hi*hi + hi*lo + lo*hi are accumulated in FP32 in tensor memory, and
-// the scale is undone in the epilogue; the split keeps about 22 bits of every
-// operand, so the result stays within the FP32 kernels' error.
+// folded value stays below 2^14) and the three products hi*hi + hi*lo + lo*hi
+// are accumulated in FP32 in tensor memory -- the large hi*hi term in its own
+// accumulator, the two small correction terms in a second one, because the
+// tensor cores' accumulation loses about a third of a unit in the last place
+// per product instruction (measured: with all three in one accumulator a
+// 1009-point row lost 1.9e-6 relative L2, 2047 points 3.7e-6; the error grows
+// with the number of instructions per accumulator).  The scale is undone in
+// the epilogue.
 //
 // Two kernels:
 //  * tcdft_fold_kernel: one warp per row (8 rows per CTA) stages the row in
 //    shared memory, finds its largest component, and writes the folded,
 //    scaled, split operand tiles (8 arrays: a, b, c, d x hi, lo) in the
-//    tensor cores' K-major core-matrix layout, one 64 KiB block per 128 rows
-//    and 32 folded indices, plus the row's inverse scale.
-//  * tcdft_mma_kernel: one CTA per (128 rows, 128 output frequencies).  A
-//    producer thread streams A (64 KiB) and cos/sin (32 KiB) blocks with bulk
-//    copies into a two-stage ring; one thread issues tcgen05.mma (M = 128,
-//    N = 128, K = 16; 12 per K step: 4 products x 3 split terms) into four
-//    FP32 accumulators that fill the SM's 512 TMEM columns; eight epilogue
-//    warps read them back with tcgen05.ld and write X_k and X_{n-k}.
+//    tensor cores' K-major core-matrix layout, one 32 KiB block per 128 rows
+//    and 16 folded indices, plus the row's inverse scale.
+//  * tcdft_mma_kernel: one CTA per (128 rows, 64 output frequencies); the
+//    CTAs of up to 8 frequency chunks of one row tile form a cluster and
+//    share every operand block through multicast bulk copies (each CTA
+//    fetches one eighth and the copy lands in all of them), while each
+//    fetches its own cos/sin block; a four-stage ring.  One thread issues
+//    tcgen05.mma (M = 128, K = 16; per step and quantity one N = 128 product
+//    into [main | correction] and one N = 64 product into the correction)
+//    into four accumulator pairs that fill the SM's 512 TMEM columns; eight
+//    epilogue warps read them back with tcgen05.ld and write X_k and X_{n-k}.
 // Every wait is bounded: on timeout the kernel records GBFFT_ERR_TIMEOUT in
 // the plan's status word, drains its own bulk copies, frees its tensor memory
 // and returns.
@@ -57,30 +64,33 @@ namespace gbfft {
 namespace {
 
 constexpr int kM = 128;                         // rows per tile = TMEM lanes
-constexpr int kKc = 32;                         // folded indices per K chunk
-constexpr int kNc = 128;                        // output frequencies per CTA
-constexpr uint32_t kTile = kM * kKc * 2;        // one [128 x 32] FP16 tile: 8 KiB
-constexpr uint32_t kABlk = 8 * kTile;           // a, b, c, d x hi, lo: 64 KiB
-constexpr uint32_t kBBlk = 4 * kTile;           // C, S x hi, lo: 32 KiB
-constexpr uint32_t kStage = kABlk + kBBlk;      // 96 KiB
+constexpr int kKc = 16;                         // folded indices per K chunk (one MMA step)
+constexpr int kNc = 64;                         // output frequencies per CTA
+constexpr uint32_t kTile = kM * kKc * 2;        // one [128 x 16] FP16 tile: 4 KiB
+constexpr uint32_t kABlk = 8 * kTile;           // a, b, c, d x hi, lo: 32 KiB
+constexpr uint32_t kBBlk = 2 * kTile;           // [C_hi; C_lo], [S_hi; S_lo]: 8 KiB
+constexpr uint32_t kStage = kABlk + kBBlk;      // 40 KiB
+constexpr int kStages = 4;
 constexpr int kFoldRows = 8;                    // rows (warps) per fold CTA
 constexpr int kMmaThreads = 320;                // producer, MMA, 8 epilogue warps
+constexpr int kMaxCluster = 8;                  // CTAs (frequency chunks) sharing operand blocks
 
-// byte offset of element (m, k) in a [rows x 32] K-major tile of core
+// byte offset of element (m, k) in a [rows x 16] K-major tile of core
 // matrices (8 rows x 16 bytes each, no swizzle): LBO 128 B along K, SBO
-// 512 B along M
+// 256 B along M
 __host__ __device__ __forceinline__ uint32_t cm_off(int m, int k) {
-  return uint32_t((m >> 3) * 512 + (k >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2);
+  return uint32_t((m >> 3) * 256 + (k >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2);
 }
 
-// shared-memory matrix descriptor: start, LBO 128 B, SBO 512 B, version 1,
+// shared-memory matrix descriptor: start, LBO 128 B, SBO 256 B, version 1,
 // no swizzle
 __device__ __forceinline__ uint64_t mat_desc(uint32_t saddr) {
-  return uint64_t((saddr >> 4) & 0x3FFF) | (uint64_t(128 >> 4) << 16) | (uint64_t(512 >> 4) << 32) |
+  return uint64_t((saddr >> 4) & 0x3FFF) | (uint64_t(128 >> 4) << 16) | (uint64_t(256 >> 4) << 32) |
          (uint64_t(1) << 46);
 }
-// instruction descriptor, kind::f16: D f32, A = B = f16, both K-major, N = 128, M = 128
-constexpr uint32_t kIdesc = (1u << 4) | ((uint32_t(kNc) >> 3) << 17) | ((uint32_t(kM) >> 4) << 24);
+// instruction descriptors, kind::f16: D f32, A = B = f16, both K-major, M = 128, N = 128 / 64
+constexpr uint32_t kIdesc128 = (1u << 4) | ((128u >> 3) << 17) | ((uint32_t(kM) >> 4) << 24);
+constexpr uint32_t kIdesc64 = (1u << 4) | ((64u >> 3) << 17) | ((uint32_t(kM) >> 4) << 24);
 
 // padded shared-memory index of element j of a staged row: one gap every
 // 8 elements keeps the fold's stride-8 reads free of bank conflicts
@@ -105,11 +115,22 @@ __global__ void __launch_bounds__(kFoldRows * 32) tcdft_fold_kernel(const PassDe
   const float2* __restrict__ in = static_cast<const float2*>(d.in) + (live ? r * d.in_cs : 0);
   const bool conj = (d.flags & F_CONJ_IN) != 0;
   float mx = 0.f;
-  for (int j = lane; j < n; j += 32) {
-    float2 x = live ? in[j] : make_float2(0.f, 0.f);
-    if (conj) x.y = -x.y;
-    sr[pidx(j)] = x;
-    mx = fmaxf(mx, fmaxf(fabsf(x.x), fabsf(x.y)));
+  // 16 loads in flight per lane before any use
+  for (int j0 = 0; j0 < n; j0 += 32 * 16) {
+    float2 xs[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int j = j0 + lane + 32 * u;
+      xs[u] = (live && j < n) ? in[j] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int j = j0 + lane + 32 * u;
+      float2 x = xs[u];
+      if (conj) x.y = -x.y;
+      if (j < n) sr[pidx(j)] = x;
+      mx = fmaxf(mx, fmaxf(fabsf(x.x), fabsf(x.y)));
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -127,8 +148,8 @@ __global__ void __launch_bounds__(kFoldRows * 32) tcdft_fold_kernel(const PassDe
   const int64_t mt = r / kM;
   const int m = int(r % kM);
   // item = (K chunk, group of 8 folded indices): 8 arrays x 16 bytes
-  for (int it = lane; it < KC * 4; it += 32) {
-    const int kc = it >> 2, g = it & 3;
+  for (int it = lane; it < KC * 2; it += 32) {
+    const int kc = it >> 1, g = it & 1;
     uint32_t w[8][4];
 #pragma unroll
     for (int q = 0; q < 8; q += 2) {
@@ -176,11 +197,11 @@ __global__ void __launch_bounds__(kFoldRows * 32) tcdft_fold_kernel(const PassDe
 }
 
 // ---- step 2: the four GEMMs and the output combination -------------------------
-__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t acc) {
+__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-      "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
+      "l"(da), "l"(db), "r"(idesc), "r"(acc)
       : "memory");
 }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -188,16 +209,33 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                    smem_u32(bar))
                : "memory");
 }
-#define GBFFT_LD16(r, addr)                                                                                \
-  asm volatile(                                                                                            \
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "   \
-      "[%16];"                                                                                             \
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),    \
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),           \
-        "=r"(r[15])                                                                                        \
-      : "r"(addr)                                                                                          \
-      : "memory")
-
+// arrive on the barrier at this offset in every CTA of `mask` once the
+// products issued so far have completed
+__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(mask)
+      : "memory");
+}
+// bulk copy delivered to the same shared-memory offset of every CTA of
+// `mask`, completing on the barrier at the same offset in each
+__device__ __forceinline__ void tma_load_1d_mc(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1], %2, [%3], "
+      "%4;" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 #define GBFFT_LD8(r, addr)                                                                   \
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"      \
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), \
@@ -205,32 +243,44 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "r"(addr)                                                                   \
                : "memory")
 
+
 // d.in: the operand blocks written by the fold (then the inverse scales);
-// d.tw: cos/sin blocks [NC][KC] of 32 KiB; d.out: output rows (row stride
-// out_cs); d.ncols rows.  Grid (row tiles, frequency chunks).
+// d.tw: cos/sin blocks [NCp][KC] of 8 KiB; d.out: output rows (row stride
+// out_cs); d.ncols rows; d.tc_nc = NCp (frequency chunks, padded to a
+// multiple of the cluster size).  Grid (row tiles, NCp); a cluster is CS
+// consecutive frequency chunks of one row tile, CS = d.W.
+//
+// Per K chunk of 16 folded indices the four quantities' products are
+//   D_q[0:128)  += A_hi(q) x [B_hi(q); B_lo(q)]   (N = 128: main | correction)
+//   D_q[64:128) += A_lo(q) x  B_hi(q)             (N = 64: correction)
+// so the large main accumulator takes one rounding per K step; the two
+// correction products (2^-11 of it) share the second half.  Accumulators at
+// columns 128q (q = aC, dS, cC, bS) fill the 512 TMEM columns.
 __global__ void __launch_bounds__(kMmaThreads, 1) tcdft_mma_kernel(const PassDesc d) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t full[2], empty[2], accf;
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], accf;
   __shared__ uint32_t s_tbase;
   __shared__ int s_fail, s_issued, s_consumed;
   // the ring starts on a 1 KiB boundary of the shared window (the launch
-  // requests 1 KiB more than the ring for this); bulk copies need 16 B and
-  // the matrix descriptors address 16-byte units
+  // requests 1 KiB more than the ring); the offset is the same in every CTA
+  // of the cluster, as multicast copies require
   unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int KC = d.tc_kc, P = d.tc_p, n = d.n;
+  const int KC = d.tc_kc, P = d.tc_p, n = d.n, CS = d.W;
   const int64_t mt = blockIdx.x;
   const int nc = int(blockIdx.y);
+  const uint32_t crank = cluster_rank();
+  const uint16_t cmask = uint16_t((1u << CS) - 1u);
   const unsigned char* A = static_cast<const unsigned char*>(d.in) + size_t(mt) * size_t(KC) * kABlk;
   const unsigned char* Bm = static_cast<const unsigned char*>(d.tw) + size_t(nc) * size_t(KC) * kBBlk;
   if (threadIdx.x == 0) {
     s_fail = 0;
     s_issued = 0;
     s_consumed = 0;
-    mbar_init(&full[0], 1);
-    mbar_init(&full[1], 1);
-    mbar_init(&empty[0], 1);
-    mbar_init(&empty[1], 1);
+    for (int i = 0; i < kStages; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], uint32_t(CS));  // one arrival per CTA of the cluster
+    }
     mbar_init(&accf, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -240,63 +290,65 @@ __global__ void __launch_bounds__(kMmaThreads, 1) tcdft_mma_kernel(const PassDes
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
+  // every CTA's barriers exist before any multicast copy or arrival lands
+  cluster_sync_all();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = s_tbase;
 
   if (warp == 0) {
     if (lane == 0) {
-      // producer: A and cos/sin blocks of chunk kc into stage kc & 1
+      // producer: operand tiles t = crank, crank + CS, ... of each chunk go to
+      // every CTA of the cluster; this CTA's own cos/sin block to itself.
+      // Chunks in a rotated order per row tile (spreads the reads of the
+      // shared cos/sin blocks over time).
+      const int k0 = int(mt % KC);
       int kc = 0;
       for (; kc < KC; ++kc) {
-        const int st = kc & 1;
-        if (kc >= 2 && !mbar_wait_bounded(&empty[st], uint32_t((kc >> 1) - 1) & 1u, d.status)) {
+        const int st = kc % kStages;
+        if (kc >= kStages &&
+            !mbar_wait_bounded(&empty[st], uint32_t(kc / kStages - 1) & 1u, d.status)) {
           atomicExch(&s_fail, 1);
           break;
         }
+        const int kk = (kc + k0) % KC;
         unsigned char* dst = smem + st * kStage;
         mbar_expect_tx(&full[st], kStage);
-        tma_load_1d(dst, A + size_t(kc) * kABlk, kABlk, &full[st]);
-        tma_load_1d(dst + kABlk, Bm + size_t(kc) * kBBlk, kBBlk, &full[st]);
+        for (int t = int(crank); t < 8; t += CS)
+          tma_load_1d_mc(dst + t * kTile, A + size_t(kk) * kABlk + size_t(t) * kTile, kTile, &full[st], cmask);
+        tma_load_1d(dst + kABlk, Bm + size_t(kk) * kBBlk, kBBlk, &full[st]);
       }
       s_issued = kc;
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      // MMA issuer: accumulators aC | dS | cC | bS at columns 0 | 128 | 256 | 384
       const int ta[4] = {0, 6, 4, 2};  // hi tile of a, d, c, b (lo = +1)
-      const int tb[4] = {0, 2, 0, 2};  // hi tile of C, S, C, S (lo = +1)
+      const int tb[4] = {0, 1, 0, 1};  // [C_hi; C_lo], [S_hi; S_lo], ...
       int kc = 0;
       for (; kc < KC; ++kc) {
-        const int st = kc & 1;
-        if (!mbar_wait_bounded(&full[st], uint32_t(kc >> 1) & 1u, d.status)) {
+        const int st = kc % kStages;
+        if (!mbar_wait_bounded(&full[st], uint32_t(kc / kStages) & 1u, d.status)) {
           atomicExch(&s_fail, 1);
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t sa = smem_u32(smem + st * kStage), sb = sa + kABlk;
 #pragma unroll
-        for (int ks = 0; ks < 2; ++ks) {
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const uint32_t acc = tmem + uint32_t(q * kNc);
-            const uint64_t ah = mat_desc(sa + ta[q] * kTile + ks * 256);
-            const uint64_t al = mat_desc(sa + (ta[q] + 1) * kTile + ks * 256);
-            const uint64_t bh = mat_desc(sb + tb[q] * kTile + ks * 256);
-            const uint64_t bl = mat_desc(sb + (tb[q] + 1) * kTile + ks * 256);
-            mma_f16(acc, ah, bh, (kc | ks) ? 1u : 0u);
-            mma_f16(acc, ah, bl, 1u);
-            mma_f16(acc, al, bh, 1u);
-          }
+        for (int q = 0; q < 4; ++q) {
+          const uint32_t acc = tmem + uint32_t(q * 128);
+          const uint64_t ah = mat_desc(sa + ta[q] * kTile), al = mat_desc(sa + (ta[q] + 1) * kTile);
+          const uint64_t bb = mat_desc(sb + tb[q] * kTile);
+          mma_f16(acc, ah, bb, kIdesc128, kc ? 1u : 0u);
+          mma_f16(acc + 64, al, bb, kIdesc64, 1u);
         }
-        mma_commit(&empty[st]);  // the stage is free once these products have read it
+        // the stage is free in every CTA once all CTAs' products have read it
+        mma_commit_mc(&empty[st], cmask);
       }
       s_consumed = kc;
       mma_commit(&accf);  // arrives when every product issued above has completed
     }
   } else {
     // epilogue: warp w reads TMEM lanes 32*(w % 4) .. +31; warps 2..5 take
-    // frequency columns 0..63 of the chunk, warps 6..9 columns 64..127
+    // frequency columns 0..31 of the chunk, warps 6..9 columns 32..63
     bool ok = mbar_wait_bounded(&accf, 0u, d.status);
     ok = ok && s_fail == 0;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -304,30 +356,36 @@ __global__ void __launch_bounds__(kMmaThreads, 1) tcdft_mma_kernel(const PassDes
     const int m = quarter * 32 + lane;
     const int64_t row = mt * kM + m;
     const int64_t mtiles = (d.ncols + kM - 1) / kM;
-    const float* rowinfo =
-        reinterpret_cast<const float*>(static_cast<const unsigned char*>(d.in) + size_t(mtiles) * size_t(KC) * kABlk);
+    const float* rowinfo = reinterpret_cast<const float*>(static_cast<const unsigned char*>(d.in) +
+                                                          size_t(mtiles) * size_t(KC) * kABlk);
     const bool live = ok && row < d.ncols;
     const float inv = live ? rowinfo[row] * ((d.flags & F_SCALE) ? float(d.scale) : 1.f) : 0.f;
     const float sgn = (d.flags & F_CONJ_OUT) ? -1.f : 1.f;
     const int h = (n - 1) / 2;
     float2* __restrict__ out = static_cast<float2*>(d.out) + (live ? row * d.out_cs : 0);
-    const int c0 = (warp < 6) ? 0 : 64;
-    const uint32_t lane_base = uint32_t(quarter * 32) << 16;
-    for (int cc = c0; cc < c0 + 64; cc += 16) {
-      uint32_t rA[16], rD[16], rC[16], rB[16];
-      // tcgen05.ld is warp-collective: every lane of the warp executes it
-      GBFFT_LD16(rA, tmem + lane_base + uint32_t(0 * kNc + cc));
-      GBFFT_LD16(rD, tmem + lane_base + uint32_t(1 * kNc + cc));
-      GBFFT_LD16(rC, tmem + lane_base + uint32_t(2 * kNc + cc));
-      GBFFT_LD16(rB, tmem + lane_base + uint32_t(3 * kNc + cc));
+    const int c0 = (warp < 6) ? 0 : 32;
+    const uint32_t lane_base = tmem + (uint32_t(quarter * 32) << 16);
+    for (int cc = c0; cc < c0 + 32; cc += 8) {
+      // main and correction halves of the four accumulators
+      uint32_t r0[8], r1[8], r2[8], r3[8], e0[8], e1[8], e2[8], e3[8];
+      GBFFT_LD8(r0, lane_base + uint32_t(0 * 128 + cc));
+      GBFFT_LD8(e0, lane_base + uint32_t(0 * 128 + 64 + cc));
+      GBFFT_LD8(r1, lane_base + uint32_t(1 * 128 + cc));
+      GBFFT_LD8(e1, lane_base + uint32_t(1 * 128 + 64 + cc));
+      GBFFT_LD8(r2, lane_base + uint32_t(2 * 128 + cc));
+      GBFFT_LD8(e2, lane_base + uint32_t(2 * 128 + 64 + cc));
+      GBFFT_LD8(r3, lane_base + uint32_t(3 * 128 + cc));
+      GBFFT_LD8(e3, lane_base + uint32_t(3 * 128 + 64 + cc));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       if (!live) continue;
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {
+      for (int c = 0; c < 8; ++c) {
         const int k = nc * kNc + cc + c;
         if (k >= P) break;
-        const float u = __uint_as_float(rA[c]), v = __uint_as_float(rD[c]);
-        const float w = __uint_as_float(rC[c]), z = __uint_as_float(rB[c]);
+        const float u = __uint_as_float(r0[c]) + __uint_as_float(e0[c]);   // aC
+        const float v = __uint_as_float(r1[c]) + __uint_as_float(e1[c]);   // dS
+        const float w = __uint_as_float(r2[c]) + __uint_as_float(e2[c]);   // cC
+        const float z = __uint_as_float(r3[c]) + __uint_as_float(e3[c]);   // bS
         out[k] = make_float2((u + v) * inv, sgn * (w - z) * inv);
         if (k >= 1 && k <= h) out[n - k] = make_float2((u - v) * inv, sgn * (w + z) * inv);
       }
@@ -339,12 +397,14 @@ __global__ void __launch_bounds__(kMmaThreads, 1) tcdft_mma_kernel(const PassDes
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int kc = s_consumed; kc < s_issued; ++kc)
-      mbar_wait_bounded(&full[kc & 1], uint32_t(kc >> 1) & 1u, d.status);
+      mbar_wait_bounded(&full[kc % kStages], uint32_t(kc / kStages) & 1u, d.status);
   }
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
   }
+  // no CTA leaves while another may still deliver copies or arrivals to it
+  cluster_sync_all();
 }
 
 size_t fold_smem(int n) { return size_t(kFoldRows) * size_t(n + (n >> 3) + 2) * sizeof(float2); }
@@ -442,9 +502,15 @@ __global__ void __launch_bounds__(kS_Threads, 2) tcdft8_kernel(const PassDesc d)
     // 1. the row's largest component
     float mx = 0.f;
     if (live)
-      for (int j = lane; j < n; j += 32) {
-        const float2 x = in[j];
-        mx = fmaxf(mx, fmaxf(fabsf(x.x), fabsf(x.y)));
+      for (int j0 = 0; j0 < n; j0 += 32 * 16) {
+        float2 xs[16];  // 16 loads in flight per lane before any use
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int j = j0 + lane + 32 * u;
+          xs[u] = j < n ? in[j] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 16; ++u) mx = fmaxf(mx, fmaxf(fabsf(xs[u].x), fabsf(xs[u].y)));
       }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -592,7 +658,6 @@ __global__ void __launch_bounds__(kS_Threads, 2) tcdft8_kernel(const PassDesc d)
   }
 }
 
-int g_tc8_ctas = 0;  // resident tcdft8 CTAs per SM (occupancy query)
 int g_tc_sms = 0;
 
 }  // namespace
@@ -601,22 +666,23 @@ cudaError_t prepare_tcdft_kernels() {
   cudaError_t e = cudaFuncSetAttribute(tcdft_fold_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        int(fold_smem(kTcDftMaxN)));
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(tcdft_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(2 * kStage + 1024));
+  e = cudaFuncSetAttribute(tcdft_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           int(kStages * kStage + 1024));
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(tcdft8_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kS_Smem + 1024));
   if (e != cudaSuccess) return e;
   int dev = 0;
   cudaGetDevice(&dev);
-  e = cudaDeviceGetAttribute(&g_tc_sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_tc8_ctas, tcdft8_kernel, kS_Threads, kS_Smem + 1024);
+  return cudaDeviceGetAttribute(&g_tc_sms, cudaDevAttrMultiProcessorCount, dev);
 }
 
 cudaError_t launch_tcdft(const PassDesc& d, cudaStream_t s) {
   if (d.ncols <= 0) return cudaSuccess;
   if (d.kernel == K_TC_DFT8) {
     const int64_t tiles = (d.ncols + kS_Rows - 1) / kS_Rows;
-    const int64_t cap = int64_t(std::max(1, g_tc_sms)) * std::max(1, g_tc8_ctas);
+    // two CTAs per SM by design (256 TMEM columns and ~105 KiB of shared
+    // memory each); CTAs beyond the resident ones simply start later
+    const int64_t cap = int64_t(std::max(1, g_tc_sms)) * 2;
     tcdft8_kernel<<<unsigned(std::min(tiles, cap)), kS_Threads, kS_Smem + 1024, s>>>(d);
     return cudaGetLastError();
   }
@@ -625,9 +691,21 @@ cudaError_t launch_tcdft(const PassDesc& d, cudaStream_t s) {
     const int64_t grid = mtiles * (kM / kFoldRows);
     tcdft_fold_kernel<<<unsigned(grid), kFoldRows * 32, fold_smem(d.n), s>>>(d);
   } else {
-    // 1 KiB beyond the ring: room to align its start (see the kernel)
-    const dim3 grid(unsigned(mtiles), unsigned(d.tc_nc));
-    tcdft_mma_kernel<<<grid, kMmaThreads, 2 * kStage + 1024, s>>>(d);
+    // 1 KiB beyond the ring: room to align its start (see the kernel); a
+    // cluster of d.W consecutive frequency chunks shares the operand blocks
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(mtiles), unsigned(d.tc_nc), 1);
+    cfg.blockDim = dim3(kMmaThreads, 1, 1);
+    cfg.dynamicSmemBytes = kStages * kStage + 1024;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 1;
+    attr[0].val.clusterDim.y = unsigned(d.W);
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, tcdft_mma_kernel, d);
   }
   return cudaGetLastError();
 }
@@ -655,7 +733,8 @@ int tcdft8_add_pass(Builder& B, int64_t n, int64_t rows, int64_t in_cs, int64_t 
       const cd w = unit_root((int64_t(p) * k2) % n2, n2);  // cos - i sin
       const double vals[2] = {w.real(), -w.imag()};
       const int hh = p / 32;
-      const uint32_t off = cm_off(k2, p % 32);  // [64 k2 x 32 K] K-major
+      // [64 k2 x 32 K] K-major core matrices: LBO 128 B (K), SBO 512 B (k2)
+      const uint32_t off = uint32_t((k2 >> 3) * 512 + ((p % 32) >> 3) * 128 + (k2 & 7) * 16 + (p % 8) * 2);
       for (int u = 0; u < 2; ++u) {
         const __half hi = __float2half_rn(float(vals[u]));
         const __half lo = __float2half_rn(float(vals[u] - double(__half2float(hi))));
@@ -694,7 +773,7 @@ int tcdft8_add_pass(Builder& B, int64_t n, int64_t rows, int64_t in_cs, int64_t 
 }
 
 size_t tcdft_scratch_bytes(int64_t n, int64_t rows) {
-  const int64_t P = n / 2 + 1, KC = (P + kKc - 1) / kKc;
+  const int64_t P = n / 2 + 1, KC = (P + kKc - 1) / kKc;  // operand blocks of 16 folded indices
   const int64_t mtiles = (rows + kM - 1) / kM;
   return size_t(mtiles) * size_t(KC) * kABlk + size_t(mtiles) * kM * sizeof(float);
 }
@@ -707,21 +786,23 @@ int tcdft_add_passes(Builder& B, int64_t n, int64_t rows, int64_t in_cs, int64_t
   if (!tcdft_available(n) || rows <= 0) return GBFFT_ERR_UNSUPPORTED;
   const int P = int(n / 2 + 1);
   const int KC = (P + kKc - 1) / kKc, NC = (P + kNc - 1) / kNc;
-  // cos/sin blocks [NC][KC]: C_hi, C_lo, S_hi, S_lo tiles of [128 k x 32 p]
-  std::vector<unsigned char> mats(size_t(NC) * size_t(KC) * kBBlk, 0);
+  // frequency chunks per cluster (1, 2, 4 or 8) and chunks padded to a multiple of it
+  const int CS = NC >= kMaxCluster ? kMaxCluster : NC > 2 ? 4 : NC;
+  const int NCp = (NC + CS - 1) / CS * CS;
+  // cos/sin blocks [NCp][KC]: tiles [C_hi; C_lo] and [S_hi; S_lo] of
+  // [128 x 16]: rows 0..63 hi and 64..127 lo of the chunk's 64 frequencies
+  std::vector<unsigned char> mats(size_t(NCp) * size_t(KC) * kBBlk, 0);
   for (int k = 0; k < P; ++k)
     for (int p = 0; p < P; ++p) {
       const cd w = unit_root((int64_t(p) * k) % n, n);  // cos - i sin
-      const double cv = w.real(), sv = -w.imag();
+      const double vals[2] = {w.real(), -w.imag()};
       const int nc = k / kNc, kc = p / kKc;
       unsigned char* blk = mats.data() + (size_t(nc) * size_t(KC) + size_t(kc)) * kBBlk;
-      const uint32_t off = cm_off(k % kNc, p % kKc);
-      const double vals[2] = {cv, sv};
       for (int u = 0; u < 2; ++u) {
         const __half hi = __float2half_rn(float(vals[u]));
         const __half lo = __float2half_rn(float(vals[u] - double(__half2float(hi))));
-        std::memcpy(blk + size_t(2 * u) * kTile + off, &hi, 2);
-        std::memcpy(blk + size_t(2 * u + 1) * kTile + off, &lo, 2);
+        std::memcpy(blk + size_t(u) * kTile + cm_off(k % kNc, p % kKc), &hi, 2);
+        std::memcpy(blk + size_t(u) * kTile + cm_off(kNc + k % kNc, p % kKc), &lo, 2);
       }
     }
   while (B.blob.size() % 256) B.blob.push_back(0);
@@ -739,7 +820,8 @@ int tcdft_add_passes(Builder& B, int64_t n, int64_t rows, int64_t in_cs, int64_t
     ps->d.tw4_n = 1;
     ps->d.tc_p = P;
     ps->d.tc_kc = KC;
-    ps->d.tc_nc = NC;
+    ps->d.tc_nc = NCp;
+    ps->d.W = CS;
   }
   f.d.kernel = K_TC_FOLD;
   f.d.in_cs = in_cs;
