@@ -52,6 +52,7 @@ enum KernelId : int {
   K_TC_FOLD = 5,  // split-FP16 dense DFT, step 1: fold rows into hi/lo FP16 operand tiles
   K_TC_DFT = 6,   // split-FP16 dense DFT, step 2: tcgen05 GEMM against cos/sin tiles
   K_TC_DFT8 = 7,  // split-FP16 rows n = 8 * n2: radix-8 on the CUDA cores, dense n2 stage on tcgen05
+  K_PLANE = 8,    // both axes of 256 x 256 planes in one pass (8-CTA cluster per plane)
 };
 
 struct StageInfo {
@@ -151,6 +152,9 @@ cudaError_t prepare_row_tc_kernels();
 cudaError_t launch_row_tc(const PassDesc& d, cudaStream_t s);
 cudaError_t launch_col4096(const PassDesc& d, bool dbl, cudaStream_t s);
 cudaError_t prepare_tcdft_kernels();
+bool plane_available(int64_t h, int64_t w, bool dbl);
+cudaError_t prepare_plane_kernels();
+cudaError_t launch_plane(const PassDesc& d, cudaStream_t s);
 cudaError_t launch_tcdft(const PassDesc& d, cudaStream_t s);
 int col_tile_width(int variant);
 

@@ -37,6 +37,8 @@ cudaError_t prepare_kernels() {
   if (e != cudaSuccess) return e;
   e = prepare_tcdft_kernels();
   if (e != cudaSuccess) return e;
+  e = prepare_plane_kernels();
+  if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(pencil_kernel<float>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   if (e != cudaSuccess) return e;
@@ -59,6 +61,7 @@ const char* pass_kernel_name(const PassDesc& d, bool dbl) {
     case K_TC_FOLD: return "tcdft_fold_kernel";
     case K_TC_DFT: return "tcdft_mma_kernel";
     case K_TC_DFT8: return "tcdft8_kernel";
+    case K_PLANE: return "plane256_kernel";
     case K_STRIDED: return str_kernel_name(d, dbl);
     default: return "pencil_kernel";
   }
@@ -70,6 +73,7 @@ cudaError_t launch_pass(const PassDesc& d, bool is_double, cudaStream_t stream) 
   if (d.kernel == K_ROW_TC) return launch_row_tc(d, stream);
   if (d.kernel == K_STRIDED) return launch_str(d, is_double, stream);
   if (d.kernel == K_TC_FOLD || d.kernel == K_TC_DFT || d.kernel == K_TC_DFT8) return launch_tcdft(d, stream);
+  if (d.kernel == K_PLANE) return launch_plane(d, stream);
   const int grid = pass_grid(d);
   if (grid <= 0) return cudaSuccess;
   const size_t smem = pass_smem_bytes(d, is_double);

@@ -745,6 +745,11 @@ bool fault_injected(const char* what) {
   return e && std::strstr(e, what) != nullptr;
 }
 
+bool feature_enabled(const char* what) {
+  const char* e = std::getenv("GBFFT_ENABLE");
+  return e && std::strstr(e, what) != nullptr;
+}
+
 bool feature_disabled(const char* what) {
   const char* e = std::getenv("GBFFT_DISABLE");
   return e && std::strstr(e, what) != nullptr;
@@ -849,6 +854,38 @@ int build_plan(gbfft_plan* p, bool dry) {
     if (st != GBFFT_OK) return st;
     if (p->passes.size() > before) first = false;
   }
+  // x and y of 256 x 256 planes (fft2D 256^2, fft3D d x 256 x 256): one
+  // cluster pass per plane (plane.cu) instead of two HBM passes
+  // Opt-in (GBFFT_ENABLE=plane): measured on GB300 the fused pass takes
+  // 99 us for the 256 planes of 256^3 against 48 + 46 us for the two passes
+  // it replaces, so the two passes stay the default.  (Split-FP16 plans keep
+  // the row pass: it is the one they move to the tensor cores.)
+  if (p->kind == GBFFT_KIND_FULL && r >= 2 && plane_available(dm[r - 2], dm[r - 1], p->dbl) &&
+      p->precision != GBFFT_SPLIT_FP16 && p->passes.size() >= 2 && feature_enabled("plane")) {
+    const PassSpec& px = p->passes[0];
+    const PassSpec& py = p->passes[1];
+    if (px.axis_final && py.axis_final && px.axis_n == dm[r - 1] && py.axis_n == dm[r - 2] && px.src == R_IN &&
+        px.dst == R_OUT && py.src == R_OUT && py.dst == R_OUT) {
+      PassSpec f;
+      std::memset(&f.d, 0, sizeof(PassDesc));
+      f.d.kernel = K_PLANE;
+      f.d.n = int(dm[r - 1]);
+      f.d.ncols = p->total / (dm[r - 1] * dm[r - 2]);
+      f.d.nbatch = f.d.nb_lo = 1;
+      f.d.in_bs = f.d.out_bs = dm[r - 1] * dm[r - 2];
+      f.d.scale = 1.0;
+      f.d.tw4_n = 1;
+      f.tw_off = int64_t(B.roots_for(dm[r - 1]));
+      f.src = R_IN;
+      f.dst = R_OUT;
+      f.axis_final = true;  // of both plane axes: no fused rotation offered
+      f.rot_ok = false;
+      f.axis_n = dm[r - 1];
+      p->passes.erase(p->passes.begin(), p->passes.begin() + 2);
+      p->passes.insert(p->passes.begin(), f);
+      p->desc += " [x+y: 256x256 planes in one cluster pass]";
+    }
+  }
   // device status word (zero) at the head of the tables
   const size_t status_off = B.add(std::vector<cd>(2, cd(0, 0)));
   // device tables
@@ -881,11 +918,10 @@ int build_plan(gbfft_plan* p, bool dry) {
       p->passes[i].d.flags |= F_L2_IN_FIRST;
     }
   }
-  // double-buffered register rows store their outputs evict_last for the
-  // next pass (fft2D 4096^2 column pass 86 -> 84 us); GBFFT_L2_KEEP=k keeps
-  // only the first k elements of each row
-  for (PassSpec& ps : p->passes)
-    if (ps.d.kernel == K_ROW) ps.d.l2_keep = ps.d.n;
+  // GBFFT_L2_KEEP=k: double-buffered register rows store the first k
+  // elements of each row evict_last for the next pass.  Off by default:
+  // measured on GB300 it took the fft2D 4096^2 column pass from 86 to 84 us
+  // but the x pass of fft3D 256^3 from 48 to 58 us.
   if (const char* kp = std::getenv("GBFFT_L2_KEEP"))
     for (PassSpec& ps : p->passes)
       if (ps.d.kernel == K_ROW) ps.d.l2_keep = std::atoll(kp);

@@ -102,6 +102,7 @@ bool fault_injected(const char* what);   // GBFFT_FAULT_INJECT=alloc,...
 // Never-reused identity of the CUDA context current on this thread (plan.cu).
 uint64_t current_context_id();
 bool feature_disabled(const char* what);  // GBFFT_DISABLE=tma,row,cluster (A/B checks)
+bool feature_enabled(const char* what);   // GBFFT_ENABLE=plane (opt-in variants)
 
 }  // namespace gbfft
 

@@ -223,6 +223,28 @@ def test_config5_shape_3d_roundtrip(gbfft_lib):
     assert float(torch.linalg.vector_norm(back - t) / torch.linalg.vector_norm(t)) < 2e-6
 
 
+@pytest.mark.parametrize("shape", [(256, 256), (5, 256, 256), (1, 256, 256)])
+def test_plane_pass_256(gbfft_lib, shape, monkeypatch):
+    """With GBFFT_ENABLE=plane, fft2D of 256 x 256 and fft3D of d x 256 x 256
+    run the x and y axes as one cluster pass per plane; every mode against
+    FP64 and the output shift (its fallback pass) against shifting the
+    result."""
+    monkeypatch.setenv("GBFFT_ENABLE", "plane")
+    g = gbfft_lib
+    rng = np.random.default_rng(len(shape))
+    x = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    plan = g.Plan(shape, kind="full", dtype=torch.complex64)
+    assert plan.pass_kernels()[0] == "plane256_kernel", plan.pass_kernels()
+    xt = torch.from_numpy(x).cuda()
+    fam = {2: "fft2D", 3: "fft3D"}[len(shape)]
+    for mode in MODES:
+        y = plan(mode, xt).cpu().numpy()
+        assert rel_l2(y, np_reference(fam, MODE_IDX[mode], x)) < 2e-6, mode
+    assert np.array_equal(plan("forward", xt, shift_out="shift").cpu().numpy(),
+                          O.shift(plan("forward", xt).cpu().numpy()))
+    assert torch.equal(xt.cpu(), torch.from_numpy(x))
+
+
 # ---- edge cases and error behaviour -----------------------------------------
 def test_empty_and_unit_arrays(gbfft_lib):
     g = gbfft_lib

@@ -33,9 +33,12 @@ def oracle_adjoint(x, H, gy):
     return gx, gH
 
 
-@pytest.mark.parametrize("shape", [(2, 16, 32, 64), (3, 8, 8, 8), (1, 32, 32, 32)])
+@pytest.mark.parametrize("shape,plane", [((2, 16, 32, 64), ""), ((3, 8, 8, 8), ""), ((1, 32, 32, 32), ""),
+                                         ((2, 3, 256, 256), ""), ((2, 3, 256, 256), "plane")])
 @pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
-def test_forward_and_adjoint_vs_oracle(gbfft_lib, shape, dtype):
+def test_forward_and_adjoint_vs_oracle(gbfft_lib, shape, plane, dtype, monkeypatch):
+    # plane: 256 x 256 planes as one cluster pass each (GBFFT_ENABLE=plane)
+    monkeypatch.setenv("GBFFT_ENABLE", plane)
     g = gbfft_lib
     rng = np.random.default_rng(sum(shape))
     x = fields(rng, shape, np.complex128)
