@@ -73,7 +73,7 @@ constexpr uint32_t kStage = kABlk + kBBlk;      // 40 KiB
 constexpr int kStages = 4;
 constexpr int kFoldRows = 8;                    // rows (warps) per fold CTA
 constexpr int kMmaThreads = 320;                // producer, MMA, 8 epilogue warps
-constexpr int kMaxCluster = 8;                  // CTAs (frequency chunks) sharing operand blocks
+constexpr int kMaxCluster = 4;                  // CTAs (frequency chunks) sharing operand blocks
 
 // byte offset of element (m, k) in a [rows x 16] K-major tile of core
 // matrices (8 rows x 16 bytes each, no swizzle): LBO 128 B along K, SBO
@@ -96,8 +96,14 @@ constexpr uint32_t kIdesc64 = (1u << 4) | ((64u >> 3) << 17) | ((uint32_t(kM) >>
 // 8 elements keeps the fold's stride-8 reads free of bank conflicts
 __device__ __forceinline__ int pidx(int j) { return j + (j >> 3); }
 
-__device__ __forceinline__ uint32_t pack_h2(__half a, __half b) {
-  return uint32_t(__half_as_ushort(a)) | (uint32_t(__half_as_ushort(b)) << 16);
+// a = hi.x + lo.x, b = hi.y + lo.y in FP16 pairs (a in the low half), both
+// rounded to nearest: one pair conversion each way instead of four scalar ones
+__device__ __forceinline__ void split_pair(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __half2 h = __floats2half2_rn(a, b);
+  const float2 hf = __half22float2(h);
+  const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
 // ---- step 1: fold, scale and split ------------------------------------------
@@ -176,13 +182,7 @@ __global__ void __launch_bounds__(kFoldRows * 32) tcdft_fold_kernel(const PassDe
         v[u][3] = dd;
       }
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const __half h0 = __float2half_rn(v[0][t]), h1 = __float2half_rn(v[1][t]);
-        const __half l0 = __float2half_rn(v[0][t] - __half2float(h0));
-        const __half l1 = __float2half_rn(v[1][t] - __half2float(h1));
-        w[2 * t][q >> 1] = pack_h2(h0, h1);
-        w[2 * t + 1][q >> 1] = pack_h2(l0, l1);
-      }
+      for (int t = 0; t < 4; ++t) split_pair(v[0][t], v[1][t], w[2 * t][q >> 1], w[2 * t + 1][q >> 1]);
     }
     unsigned char* blk = A + (size_t(mt) * size_t(KC) + size_t(kc)) * kABlk + cm_off(m, g * 8);
 #pragma unroll
@@ -493,6 +493,7 @@ __global__ void __launch_bounds__(kS_Threads, 2) tcdft8_kernel(const PassDesc d)
   const float osc = (d.flags & F_SCALE) ? float(d.scale) : 1.f;
   const float sgn = (d.flags & F_CONJ_OUT) ? -1.f : 1.f;
   const int64_t tiles = (d.ncols + kS_Rows - 1) / kS_Rows;
+  const bool vec_rows = ((reinterpret_cast<uintptr_t>(d.in) & 15) == 0) && (d.in_cs % 2 == 0);
   uint32_t phase = 0;
   bool fail = false;
   for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
@@ -501,7 +502,21 @@ __global__ void __launch_bounds__(kS_Threads, 2) tcdft8_kernel(const PassDesc d)
     const float2* __restrict__ in = static_cast<const float2*>(d.in) + (live ? row * d.in_cs : 0);
     // 1. the row's largest component
     float mx = 0.f;
-    if (live)
+    if (live && vec_rows) {
+      // pairs of elements as 16-byte loads (n is even, rows 16-byte aligned)
+      const float4* in4 = reinterpret_cast<const float4*>(in);
+      for (int j0 = 0; j0 < n / 2; j0 += 32 * 16) {
+        float4 xs[16];  // 16 loads in flight per lane before any use
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int j = j0 + lane + 32 * u;
+          xs[u] = j < n / 2 ? in4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 16; ++u)
+          mx = fmaxf(mx, fmaxf(fmaxf(fabsf(xs[u].x), fabsf(xs[u].y)), fmaxf(fabsf(xs[u].z), fabsf(xs[u].w))));
+      }
+    } else if (live) {
       for (int j0 = 0; j0 < n; j0 += 32 * 16) {
         float2 xs[16];  // 16 loads in flight per lane before any use
 #pragma unroll
@@ -512,6 +527,7 @@ __global__ void __launch_bounds__(kS_Threads, 2) tcdft8_kernel(const PassDesc d)
 #pragma unroll
         for (int u = 0; u < 16; ++u) mx = fmaxf(mx, fmaxf(fabsf(xs[u].x), fabsf(xs[u].y)));
       }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     int sh = 0;
@@ -576,9 +592,7 @@ __global__ void __launch_bounds__(kS_Threads, 2) tcdft8_kernel(const PassDesc d)
               const float f = (q == 0) ? x1.x + x2.x : (q == 1) ? x1.x - x2.x : (q == 2) ? x1.y + x2.y : x1.y - x2.y;
               v[u] = ((q & 1) && !pair) ? 0.f : f;
             }
-            const __half h0 = __float2half_rn(v[0]), h1 = __float2half_rn(v[1]);
-            hi[k1 >> 1] = pack_h2(h0, h1);
-            lo[k1 >> 1] = pack_h2(__float2half_rn(v[0] - __half2float(h0)), __float2half_rn(v[1] - __half2float(h1)));
+            split_pair(v[0], v[1], hi[k1 >> 1], lo[k1 >> 1]);
           }
           *reinterpret_cast<uint4*>(dst + (2 * q) * kS_ATile) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
           *reinterpret_cast<uint4*>(dst + (2 * q + 1) * kS_ATile) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
