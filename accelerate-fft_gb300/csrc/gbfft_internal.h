@@ -110,10 +110,6 @@ struct PassDesc {
   // K_TC_FOLD / K_TC_DFT: folded length P (= floor(n/2) + 1), K chunks of
   // 32 and output chunks of 128 frequencies covering it
   int tc_p, tc_kc, tc_nc;
-  // K_ROW double-buffered rows with F_L2_OUT_LAST: outputs of axis index
-  // k < l2_keep are stored evict_last (the rest plainly), so that a chosen
-  // share of the intermediate stays in L2 for the next pass
-  int64_t l2_keep;
 };
 
 // Address offset of F_ROT_OUT for axis index l (0 without the flag).

@@ -918,13 +918,6 @@ int build_plan(gbfft_plan* p, bool dry) {
       p->passes[i].d.flags |= F_L2_IN_FIRST;
     }
   }
-  // GBFFT_L2_KEEP=k: double-buffered register rows store the first k
-  // elements of each row evict_last for the next pass.  Off by default:
-  // measured on GB300 it took the fft2D 4096^2 column pass from 86 to 84 us
-  // but the x pass of fft3D 256^3 from 48 to 58 us.
-  if (const char* kp = std::getenv("GBFFT_L2_KEEP"))
-    for (PassSpec& ps : p->passes)
-      if (ps.d.kernel == K_ROW) ps.d.l2_keep = std::atoll(kp);
   unsigned char* base = static_cast<unsigned char*>(p->d_tables);
   p->d_status = reinterpret_cast<int*>(base + status_off);
   const bool tma = !feature_disabled("tma");

@@ -95,8 +95,6 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_kernel(const PassDe
                                                    RL<Rs...>{});
   if (!ok) return;
   const T s = T(d.scale);
-  const int64_t keep = (fl & F_L2_OUT_LAST) ? d.l2_keep : 0;
-  const uint64_t pol = keep > 0 ? l2_policy_last() : 0;
 #pragma unroll
   for (int q = 0; q < E / RZ; ++q)
 #pragma unroll
@@ -105,11 +103,7 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_kernel(const PassDe
       if (fl & F_SCALE) x = cscale(x, s);
       if (fl & F_CONJ_OUT) x.y = -x.y;
       const int k = t + TH * (q + r * (E / RZ));
-      C* o = out + k + rot_delta(d, k);
-      if (k < keep)
-        st_l2hint(o, x, pol);
-      else
-        *o = x;
+      out[k + rot_delta(d, k)] = x;
     }
 }
 
