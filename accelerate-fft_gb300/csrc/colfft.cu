@@ -629,6 +629,181 @@ struct ColR16Cfg {
   }
 };
 
+// Leaner form of the radix-16 kernel (Complex Float), same split and data
+// flow, fewer instructions per element:
+//   * twiddles come from two shared-memory tables filled at the start,
+//     W_4096^(b*K1) for the CTA's 32 b ([bl][K1]) and W_256^(gamma*kappa)
+//     ([gamma][kappa]), read two at a time as 16-byte vectors, instead of
+//     being built by products of three table entries;
+//   * the two K1 values a thread sends to one CTA go as one 16-byte
+//     st.async (receive layout [b][x][K1l]), 8 pushes per thread instead of 16;
+//   * the flag handling (conjugation, scaling, output rotation, L2 hint) is
+//     hoisted out of the element loops into uniform branches.
+__device__ __forceinline__ void st_async2(uint32_t addr, float2 a, float2 b, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+                   addr),
+               "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "r"(bar)
+               : "memory");
+}
+
+// v[k] *= tab[k], k = 1..15 (tab[0] = 1): eight 16-byte shared loads
+__device__ __forceinline__ void apply_table16(float2 (&v)[16], const float2* tab) {
+  const float4* t4 = reinterpret_cast<const float4*>(tab);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float4 p = t4[j];
+    if (j > 0) v[2 * j] = cmul(v[2 * j], make_float2(p.x, p.y));
+    v[2 * j + 1] = cmul(v[2 * j + 1], make_float2(p.z, p.w));
+  }
+}
+
+template <int W>
+constexpr size_t col_r16b_smem() {
+  return size_t(512) * W * sizeof(float2) + size_t(512 + 256) * sizeof(float2);
+}
+
+template <int W, int MINB>
+__global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
+    colfft4096_r16b_kernel(const PassDesc d) {
+  using C = float2;
+  static_assert(W == 8 || W == 16, "whole values of q per warp");
+  constexpr uint32_t kRecvBytes = 4096u * W / 8u * sizeof(C);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* rv = reinterpret_cast<C*>(smem_raw);  // [b][x][K1l], reused for the stage-2 exchange
+  C* t1 = rv + 512 * W;                     // [bl][K1]: W_4096^((32r + bl) * K1)
+  C* t2 = t1 + 512;                         // [gamma][kappa]: W_256^(gamma * kappa)
+  __shared__ __align__(8) uint64_t rbar;
+  const int r = int(cg::this_cluster().block_rank());
+  const int64_t tile = int64_t(blockIdx.x) >> 3;
+  const int64_t tpb = d.ncols / W;
+  const int64_t bo = tile / tpb;
+  const int64_t x0 = (tile - bo * tpb) * W;
+  const C* __restrict__ w = static_cast<const C*>(d.tw);
+  const uint32_t fl = d.flags;
+  const int tid = threadIdx.x;
+  const int x = tid % W;
+  const int q = tid / W;  // 0..31
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&rbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  cluster_arrive_release();
+
+  // twiddle table entries first (their loads overlap the column loads).
+  // Every table row is filled and read by the threads of one warp: row q of
+  // t1 by the threads (x, q), row gamma of t2 by the threads with q >> 1 =
+  // gamma (a warp holds 32 / W whole values of q, W >= 8), so a warp barrier
+  // orders the fills before the reads.
+  C e1[16 / W], e2 = make_float2(1.f, 0.f);
+#pragma unroll
+  for (int i = 0; i < 16 / W; ++i) e1[i] = tw_at(w, ((32 * r + q) * (x + W * i)) & 4095);
+  const int k2 = x + W * (q & 1);
+  if (k2 < 16) e2 = tw_at(w, (16 * (q >> 1) * k2) & 4095);
+
+  // ---- phase 1: thread (x, bl = q): DFT-16 over a of column x, b = 32r + q
+  const int b = 32 * r + q;
+  C v[16];
+  {
+    const C* __restrict__ in = static_cast<const C*>(d.in) + bo * d.in_bs + x0 + int64_t(b) * d.in_es + x;
+    const int64_t as = 256 * d.in_es;
+    if (fl & F_L2_IN_FIRST) {
+      const uint64_t pol = l2_policy_first();
+#pragma unroll
+      for (int a = 0; a < 16; ++a) v[a] = ld_l2hint(in + a * as, pol);
+    } else {
+#pragma unroll
+      for (int a = 0; a < 16; ++a) v[a] = in[a * as];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 16 / W; ++i) t1[16 * q + x + W * i] = e1[i];
+  if (k2 < 16) t2[16 * (q >> 1) + k2] = e2;
+  if (fl & F_CONJ_IN) {
+#pragma unroll
+    for (int a = 0; a < 16; ++a) v[a].y = -v[a].y;
+  }
+  dft16(v);
+  __syncwarp();  // this warp's twiddle table rows
+  apply_table16(v, t1 + 16 * q);  // W^(b*K1)
+  if (tid == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&rbar)),
+                 "r"(kRecvBytes)
+                 : "memory");
+  }
+  cluster_wait_acquire();
+  const uint32_t bar0 = smem_u32(&rbar);
+  {
+    const uint32_t dst = smem_u32(rv) + uint32_t((b * W + x) * 2 * sizeof(C));
+#pragma unroll
+    for (int j = 0; j < 8; ++j) st_async2(mapa_u32(dst, uint32_t(j)), v[2 * j], v[2 * j + 1], mapa_u32(bar0, uint32_t(j)));
+  }
+  // ---- phase 2: wait for the 256 b of this CTA's two K1 values ------------
+  bool ok = false;
+  for (uint32_t it = 0; it < kColWaitLimit && !ok; ++it) {
+    uint32_t t;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(t)
+        : "r"(bar0)
+        : "memory");
+    ok = t != 0;
+  }
+  if (!ok && d.status) atomicExch(d.status, GBFFT_ERR_TIMEOUT_DEVICE);
+  // stage 2: thread (x, K1l = q & 1, gamma = q >> 1): DFT-16 over beta
+  const int K1l = q & 1;
+  const int gamma = q >> 1;
+  C* col = rv + 2 * x + K1l;  // element (row, x, K1l) at col[row * 2W]
+#pragma unroll
+  for (int beta = 0; beta < 16; ++beta) v[beta] = col[(16 * beta + gamma) * 2 * W];
+  dft16(v);
+  apply_table16(v, t2 + 16 * gamma);  // W_256^(gamma*kappa)
+  __syncthreads();  // every stage-2 read of the receive buffer is done
+#pragma unroll
+  for (int kappa = 0; kappa < 16; ++kappa) col[(kappa * 16 + gamma) * 2 * W] = v[kappa];
+  __syncthreads();
+  // stage 3: thread (x, K1l, kappa = q >> 1): DFT-16 over gamma
+  const int kappa = q >> 1;
+#pragma unroll
+  for (int g = 0; g < 16; ++g) v[g] = col[(kappa * 16 + g) * 2 * W];
+  dft16(v);
+  if (fl & (F_SCALE | F_CONJ_OUT)) {
+    const float s = (fl & F_SCALE) ? float(d.scale) : 1.0f;
+    const float cy = (fl & F_CONJ_OUT) ? -s : s;
+#pragma unroll
+    for (int lambda = 0; lambda < 16; ++lambda) v[lambda] = make_float2(v[lambda].x * s, v[lambda].y * cy);
+  }
+  const int K1 = 2 * r + K1l;
+  C* __restrict__ out = static_cast<C*>(d.out) + bo * d.out_bs + x0 + x;
+  const int64_t oes = d.out_es;
+  if (fl & F_ROT_OUT) {
+#pragma unroll
+    for (int lambda = 0; lambda < 16; ++lambda) {
+      const int l = K1 + 16 * kappa + 256 * lambda;
+      out[int64_t(l) * oes + rot_delta(d, l)] = v[lambda];
+    }
+  } else {
+    C* o = out + int64_t(K1 + 16 * kappa) * oes;
+    const int64_t ls = 256 * oes;
+#pragma unroll
+    for (int lambda = 0; lambda < 16; ++lambda) o[lambda * ls] = v[lambda];
+  }
+}
+
+template <int W, int MINB>
+struct ColR16bCfg {
+  static constexpr int threads = 32 * W;
+  static cudaError_t prepare() {
+    return cudaFuncSetAttribute(colfft4096_r16b_kernel<W, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(col_r16b_smem<W>()));
+  }
+  static cudaError_t launch(const PassDesc& d, cudaStream_t s) {
+    const int64_t tiles = (d.ncols / W) * d.nbatch;
+    colfft4096_r16b_kernel<W, MINB><<<unsigned(tiles * 8), threads, col_r16b_smem<W>(), s>>>(d);
+    return cudaGetLastError();
+  }
+};
+
 template <typename T, int W> size_t col_smem() { return size_t(8) * col_gp<W>() * sizeof(typename CxT<T>::type); }
 
 template <typename T, int W, int U, int MINB>
@@ -727,6 +902,15 @@ struct ColR16TmaCfg {
   X(14, float, 16, 1)            \
   X(15, float, 8, 3)
 
+// lean radix-16 variants, Complex Float only (W, min CTAs per SM); 18 is the
+// default: on the 4096 x 4096 column pass 77.8 us against 86.0 us for 9
+// (16: 92.2, 19: 84.0-86.0, 10: 94.2, 8: 107.9)
+#define GBFFT_COLR16B_TABLE(X) \
+  X(16, 16, 2)                 \
+  X(17, 8, 5)                  \
+  X(18, 8, 4)                  \
+  X(19, 8, 3)
+
 }  // namespace
 
 cudaError_t prepare_col_kernels() {
@@ -747,13 +931,17 @@ cudaError_t prepare_col_kernels() {
   if (e == cudaSuccess) e = ColR16TmaCfg<T, W, MINB>::prepare();
   GBFFT_COLR16TMA_TABLE(X)
 #undef X
+#define X(V, W, MINB) \
+  if (e == cudaSuccess) e = ColR16bCfg<W, MINB>::prepare();
+  GBFFT_COLR16B_TABLE(X)
+#undef X
   if (e == cudaSuccess) e = ColCfg<double, 16, 2, 1>::prepare();
   return e;
 }
 
 int col_tile_width(int variant) {
   switch (variant) {
-    case 0: case 3: case 6: case 9: case 11: case 13: case 14: return 16;
+    case 0: case 3: case 6: case 9: case 11: case 13: case 14: case 16: return 16;
     case 12: return 32;
     default: return 8;
   }
@@ -776,6 +964,10 @@ cudaError_t launch_col4096(const PassDesc& d, bool dbl, cudaStream_t s) {
 #define X(V, T, W, MINB) \
   if (d.col_variant == V) return ColR16TmaCfg<T, W, MINB>::launch(d, s);
   GBFFT_COLR16TMA_TABLE(X)
+#undef X
+#define X(V, W, MINB) \
+  if (d.col_variant == V) return ColR16bCfg<W, MINB>::launch(d, s);
+  GBFFT_COLR16B_TABLE(X)
 #undef X
   return cudaErrorInvalidValue;
 }

@@ -53,7 +53,8 @@ const char* pass_kernel_name(const PassDesc& d, bool dbl) {
       if (d.row_variant & 1) return "rowfft1_kernel";
       return (d.use_tma && d.in_cs == d.n && d.out_cs == d.n) ? "rowfft_tma_kernel" : "rowfft_kernel";
     case K_COL4096:
-      return (d.col_variant >= 14 && d.use_tma && d.in_cs == 1) ? "colfft4096_r16_tma_kernel"
+      return d.col_variant >= 16 ? "colfft4096_r16b_kernel"
+           : (d.col_variant >= 14 && d.use_tma && d.in_cs == 1) ? "colfft4096_r16_tma_kernel"
            : d.col_variant >= 8 ? "colfft4096_r16_kernel"
            : d.col_variant >= 4 ? "colfft4096_push_kernel"
                                 : "colfft4096_kernel";

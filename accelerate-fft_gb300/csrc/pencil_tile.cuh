@@ -29,7 +29,7 @@ __device__ __forceinline__ C ldg_c(const C* p) {
 // One Stockham stage of radix R over every pencil of the tile:
 // butterfly j reads src[j + r*n/R], twiddles by W_{Ns*R}^{(j mod Ns)*r},
 // and writes dst[(j/Ns)*Ns*R + (j mod Ns) + r*Ns].  The stage twiddle table
-// holds W_{Ns*R}^{p*r} at p*Rp + r, Rp = R rounded up to even.
+// holds W_{Ns*R}^{p*r}, 0 < r < R, at (r - 1)*Ns + p.
 template <int R, typename C>
 __device__ __forceinline__ void stage(const C* __restrict__ src, C* __restrict__ dst,
                                       const C* __restrict__ tw, int n, int Ns, int W, int pitch) {
@@ -46,9 +46,9 @@ __device__ __forceinline__ void stage(const C* __restrict__ src, C* __restrict__
     for (int r = 0; r < R; ++r) v[r] = s[spad(j + r * nb)];
     const int p = j - int(div_ns.div(uint32_t(j))) * Ns;
     if (Ns > 1) {
-      const C* t = tw + p * (R + (R & 1));
+      const C* t = tw + p;
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], ldg_c(t + r));
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], ldg_c(t + (r - 1) * Ns));
     }
     dft<R>(v);
     const int base = (j - p) * R + p;

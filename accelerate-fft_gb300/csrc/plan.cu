@@ -213,12 +213,13 @@ bool Builder::stages_for(int n, PassSpec& ps) {
   if (it == stage_cache.end()) {
     std::vector<cd> t;
     int64_t Ns = 1;
+    // stage (Ns, R): W_{Ns*R}^{p*r}, 0 < r < R, at (r - 1)*Ns + p (p fastest:
+    // the butterflies of neighbouring threads read neighbouring entries)
     for (size_t s = 0; s < f.size(); ++s) {
       offs[s] = int(t.size());
       const int R = f[s];
-      const int Rp = R + (R & 1);  // even stride: each butterfly's twiddles start 16-byte aligned
-      for (int64_t p = 0; p < Ns; ++p)
-        for (int r = 0; r < Rp; ++r) t.push_back(unit_root(p * r, Ns * R));
+      for (int r = 1; r < R; ++r)
+        for (int64_t p = 0; p < Ns; ++p) t.push_back(unit_root(p * r, Ns * R));
       Ns *= R;
     }
     if (t.empty()) t.push_back(cd(1, 0));
@@ -937,8 +938,8 @@ int build_plan(gbfft_plan* p, bool dry) {
     ps.d.row_variant = tc.row_variant >= 0 ? tc.row_variant : (ps.d.kernel == K_ROW && !p->dbl) ? 0 : 1;
     ps.d.col_variant = tc.col_variant;
     if (const char* rv = std::getenv("GBFFT_ROW_VARIANT")) ps.d.row_variant = std::atoi(rv) & 1;
-    if (const char* cv = std::getenv("GBFFT_COL_VARIANT")) ps.d.col_variant = std::atoi(cv) & 15;
-    if (ps.d.col_variant > 15) ps.d.col_variant = 9;
+    if (const char* cv = std::getenv("GBFFT_COL_VARIANT")) ps.d.col_variant = std::atoi(cv) & 31;
+    if (ps.d.col_variant > 19) ps.d.col_variant = 9;
     if (ps.d.kernel == K_COL4096 && ps.d.ncols % col_tile_width(ps.d.col_variant) != 0)
       ps.d.col_variant = 8;  // 8-column tiles
     if (ps.tw_off >= 0) ps.d.tw = base + ps.tw_off;
@@ -947,6 +948,13 @@ int build_plan(gbfft_plan* p, bool dry) {
     if (ps.chirp_off >= 0) ps.d.chirp = base + ps.chirp_off;
     if (ps.filter_off >= 0) ps.d.filter = base + ps.filter_off;
   }
+  for (const PassSpec& ps : p->passes)
+    if (ps.d.kernel == K_COL4096) {  // columns per cluster tile of the variant that runs
+      char cb[40];
+      std::snprintf(cb, sizeof cb, " cluster-columns=%d", p->dbl ? 16 : col_tile_width(ps.d.col_variant));
+      p->desc += cb;
+      break;
+    }
   if (tc.tuned) {
     char tb[96];
     std::snprintf(tb, sizeof tb, " tuned(row=%d%s col=%d split=%d strtma=%d bluepad=%d rowk=%d)", tc.row_variant,

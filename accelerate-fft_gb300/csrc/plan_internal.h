@@ -69,7 +69,7 @@ struct Builder {
 struct TuneChoice {
   int row_variant = -1;  // contiguous rows: 1 single-buffered, 0 double-buffered, -1 by kernel
   int row_tma = 0;      //   with row_variant 0: stream rows with cp.async.bulk
-  int col_variant = 9;  // 4096-point strided axes: cluster kernel variant
+  int col_variant = 18;  // 4096-point strided axes: cluster kernel variant (colfft.cu)
   int split_rank = 0;   // four-step axes: k-th best (n1, n2) factorisation
   int str_tma = 1;      // strided passes: tensor-copy-fed persistent kernel
   int blue_pad = 1;     // Bluestein padding: 1 power of two when cheaper, 0 smallest smooth m,

@@ -8,8 +8,8 @@
 // bits 4-6) that keeps every access pattern of these stages conflict-free and
 // keeps element pairs adjacent, so the first stage's outputs are written as
 // 16-byte vectors.  The radix list is a template parameter equal to the
-// planner's factorisation (factor_device), so both kernels share the stage
-// twiddle table layout of the generic pencil kernel.
+// planner's factorisation (factor_device), so the kernels share the stage
+// twiddle table layout ([r - 1][p] per stage) of the generic pencil kernel.
 //
 // Two variants:
 //  * rowfft_kernel: one chunk of ROWS rows per CTA, the first stage loading
@@ -44,7 +44,7 @@ __device__ __forceinline__ void row_stages2(C (&v)[E], C* bufs, const C* __restr
     __syncthreads();
     constexpr int R2 = rl_first(RL<Rest...>{});
     row_read<N, E, R2>(v, b, t);
-    row_stages2<N, E, NS * R, OFF + NS * even_up<R>(), 1 - BUF, PITCH>(v, bufs, tw, t, RL<Rest...>{});
+    row_stages2<N, E, NS * R, OFF + tw_entries<R>(NS), 1 - BUF, PITCH>(v, bufs, tw, t, RL<Rest...>{});
   }
 }
 
@@ -60,7 +60,7 @@ __device__ __forceinline__ void row_stages1(C (&v)[E], C* b, const C* __restrict
     constexpr int R2 = rl_first(RL<Rest...>{});
     row_read<N, E, R2>(v, b, t);
     __syncthreads();
-    row_stages1<N, E, NS * R, OFF + NS * even_up<R>()>(v, b, tw, t, RL<Rest...>{});
+    row_stages1<N, E, NS * R, OFF + tw_entries<R>(NS)>(v, b, tw, t, RL<Rest...>{});
   }
 }
 
@@ -81,30 +81,39 @@ __global__ void __launch_bounds__(ROWS*(N / E), MINB) rowfft_kernel(const PassDe
   const C* __restrict__ in = static_cast<const C*>(d.in) + row * d.in_cs;
   C* __restrict__ out = static_cast<C*>(d.out) + row * d.out_cs;
 
+  // the flag handling sits in uniform branches outside the element loops
   C v[E];
 #pragma unroll
   for (int q = 0; q < E / R0; ++q)
 #pragma unroll
-    for (int r = 0; r < R0; ++r) {
-      C x = cmake<C>(T(0), T(0));
-      if (ok) x = in[t + TH * (q + r * (E / R0))];
-      if (fl & F_CONJ_IN) x.y = -x.y;
-      v[q * R0 + r] = x;
-    }
+    for (int r = 0; r < R0; ++r) v[q * R0 + r] = ok ? in[t + TH * (q + r * (E / R0))] : cmake<C>(T(0), T(0));
+  if (fl & F_CONJ_IN) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e].y = -v[e].y;
+  }
   row_stages2<N, E, 1, 0, 0, ROWS * row_pitch<N>()>(v, bufs, static_cast<const C*>(d.tw), t,
                                                    RL<Rs...>{});
   if (!ok) return;
-  const T s = T(d.scale);
+  if (fl & (F_SCALE | F_CONJ_OUT)) {
+    const T s = (fl & F_SCALE) ? T(d.scale) : T(1);
+    const T cy = (fl & F_CONJ_OUT) ? -s : s;
 #pragma unroll
-  for (int q = 0; q < E / RZ; ++q)
+    for (int e = 0; e < E; ++e) v[e] = cmake<C>(v[e].x * s, v[e].y * cy);
+  }
+  if (fl & F_ROT_OUT) {
 #pragma unroll
-    for (int r = 0; r < RZ; ++r) {
-      C x = v[q * RZ + r];
-      if (fl & F_SCALE) x = cscale(x, s);
-      if (fl & F_CONJ_OUT) x.y = -x.y;
-      const int k = t + TH * (q + r * (E / RZ));
-      out[k + rot_delta(d, k)] = x;
-    }
+    for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+      for (int r = 0; r < RZ; ++r) {
+        const int k = t + TH * (q + r * (E / RZ));
+        out[k + rot_delta(d, k)] = v[q * RZ + r];
+      }
+  } else {
+#pragma unroll
+    for (int q = 0; q < E / RZ; ++q)
+#pragma unroll
+      for (int r = 0; r < RZ; ++r) out[t + TH * (q + r * (E / RZ))] = v[q * RZ + r];
+  }
 }
 
 // Variant with one exchange buffer (half the shared memory, two barriers per
@@ -448,7 +457,7 @@ __device__ __forceinline__ void row_compute_tc(float2 (&v)[E], const float2* __r
     if constexpr (NS > 1) {
       const int p = t % NS;
       float2 w[17];
-      derive_tw<16>(w, tw + p * 16);
+      derive_tw<16, NS>(w, tw + p);
 #pragma unroll
       for (int r = 1; r < 16; ++r) v[r] = cmul(v[r], w[r]);
     }
@@ -468,7 +477,7 @@ __device__ __forceinline__ void row_stages_tc(float2 (&v)[E], float2* b, const f
     constexpr int R2 = rl_first(RL<Rest...>{});
     row_read<N, E, R2>(v, b, t);
     __syncthreads();
-    row_stages_tc<N, E, NS * R, OFF + NS * even_up<R>()>(v, b, tw, t, c, RL<Rest...>{});
+    row_stages_tc<N, E, NS * R, OFF + tw_entries<R>(NS)>(v, b, tw, t, c, RL<Rest...>{});
   }
 }
 

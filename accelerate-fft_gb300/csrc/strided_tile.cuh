@@ -17,38 +17,32 @@ template <int R> constexpr int rl_last(RL<R>) { return R; }
 template <int R, int R2, int... Rest> constexpr int rl_last(RL<R, R2, Rest...>) {
   return rl_last(RL<R2, Rest...>{});
 }
-template <int R> constexpr int even_up() { return R + (R & 1); }
+// entries of the stage twiddle table of stage (NS, R)
+template <int R> constexpr int tw_entries(int ns) { return (R - 1) * ns; }
 // row pitch of the exchange buffers: a multiple of 16 so the swizzle stays
 // inside the row and 16-byte stores stay aligned
 template <int N> constexpr int row_pitch() { return (N + 15) & ~15; }
 
-// twiddles W^{p*r}, r < R, of one butterfly (table stride even_up(R))
-template <int R>
-__device__ __forceinline__ void load_tw(float2 (&w)[R + 1], const float2* __restrict__ base) {
-  const float4* b4 = reinterpret_cast<const float4*>(base);
+// Stage twiddle tables: stage (NS, R) holds W_{NS*R}^{p*r}, 0 < r < R,
+// p < NS, at (r - 1) * NS + p -- (R - 1) * NS entries, p fastest, so the
+// butterflies of consecutive threads (consecutive p) read consecutive
+// entries.  `base` below is the stage table advanced by the butterfly's p.
+template <int R, int NS, typename C>
+__device__ __forceinline__ void load_tw(C (&w)[R + 1], const C* __restrict__ base) {
 #pragma unroll
-  for (int k = 0; k < even_up<R>() / 2; ++k) {
-    const float4 q = __ldg(b4 + k);
-    w[2 * k] = make_float2(q.x, q.y);
-    if (2 * k + 1 <= R) w[2 * k + 1] = make_float2(q.z, q.w);
-  }
-}
-template <int R>
-__device__ __forceinline__ void load_tw(double2 (&w)[R + 1], const double2* __restrict__ base) {
-#pragma unroll
-  for (int r = 1; r < R; ++r) w[r] = __ldg(base + r);
+  for (int r = 1; r < R; ++r) w[r] = __ldg(base + (r - 1) * NS);
 }
 
 // Complex Float twiddles derived from a few table entries: W^p, W^4p, W^8p
 // are loaded and the other powers formed with at most three complex
-// multiplications (a few ulp), which keeps the L1 traffic per butterfly at
-// three 8-byte loads instead of R-1.
-template <int R>
+// multiplications (a few ulp), three 8-byte loads per butterfly instead of
+// R - 1.
+template <int R, int NS>
 __device__ __forceinline__ void derive_tw(float2 (&w)[R + 1], const float2* __restrict__ base) {
   if constexpr (R == 16) {
-    w[1] = __ldg(base + 1);
-    w[4] = __ldg(base + 4);
-    w[8] = __ldg(base + 8);
+    w[1] = __ldg(base);
+    w[4] = __ldg(base + 3 * NS);
+    w[8] = __ldg(base + 7 * NS);
     w[2] = cmul(w[1], w[1]);
     w[3] = cmul(w[2], w[1]);
     w[5] = cmul(w[4], w[1]);
@@ -62,15 +56,15 @@ __device__ __forceinline__ void derive_tw(float2 (&w)[R + 1], const float2* __re
     w[14] = cmul(w[12], w[2]);
     w[15] = cmul(w[12], w[3]);
   } else if constexpr (R == 8) {
-    w[1] = __ldg(base + 1);
-    w[4] = __ldg(base + 4);
+    w[1] = __ldg(base);
+    w[4] = __ldg(base + 3 * NS);
     w[2] = cmul(w[1], w[1]);
     w[3] = cmul(w[2], w[1]);
     w[5] = cmul(w[4], w[1]);
     w[6] = cmul(w[4], w[2]);
     w[7] = cmul(w[4], w[3]);
   } else {
-    load_tw<R>(w, base);
+    load_tw<R, NS>(w, base);
   }
 }
 
@@ -85,9 +79,9 @@ __device__ __forceinline__ void row_compute(C (&v)[E], const C* __restrict__ tw,
       const int p = j % NS;
       C w[R + 1];
       if constexpr (sizeof(C) == 8)
-        derive_tw<R>(w, tw + p * even_up<R>());
+        derive_tw<R, NS>(w, tw + p);
       else
-        load_tw<R>(w, tw + p * even_up<R>());
+        load_tw<R, NS>(w, tw + p);
 #pragma unroll
       for (int r = 1; r < R; ++r) v[q * R + r] = cmul(v[q * R + r], w[r]);
     }
@@ -174,7 +168,7 @@ __device__ __forceinline__ void str_stages(C (&v)[E], C* b, const C* __restrict_
     constexpr int R2 = rl_first(RL<Rest...>{});
     str_read<N, E, R2, W>(v, b, t, x);
     __syncthreads();
-    str_stages<N, E, NS * R, OFF + NS * even_up<R>(), W>(v, b, tw, t, x, RL<Rest...>{});
+    str_stages<N, E, NS * R, OFF + tw_entries<R>(NS), W>(v, b, tw, t, x, RL<Rest...>{});
   }
 }
 

@@ -243,7 +243,7 @@ int autotune_plan(int rank, const int64_t* dims, int kind, int dtype, int precis
     const Knob knobs[] = {
         {&TuneChoice::row_variant, {1, 0}, has_kernel(p0, K_ROW) || has_kernel(p0, K_ROW_TC)},
         {&TuneChoice::row_tma, {1, 0}, has_kernel(p0, K_ROW)},
-        {&TuneChoice::col_variant, {9, 11, 13, 8, 10, 15, 14}, has_kernel(p0, K_COL4096)},
+        {&TuneChoice::col_variant, {18, 9, 17, 19, 16, 11, 13, 8, 10, 15, 14}, has_kernel(p0, K_COL4096)},
         {&TuneChoice::split_rank, {0, 1, 2}, has_flag(p0, F_TW4)},
         {&TuneChoice::str_tma, {1, 0}, has_kernel(p0, K_STRIDED)},
         {&TuneChoice::blue_pad, {1, 0}, has_flag(p0, F_CHIRP_IN)},

@@ -19,6 +19,7 @@ import ctypes
 import json
 import math
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -384,16 +385,19 @@ def measure_gbfft(args, wl, headline=True):
     ach_tr = bytes_pass * len(ops) / (ms * 1e-3) / 1e9
 
     # the access pattern's own ceiling (outside the timed region): a plain
-    # copy of the same array in 16-column tiles over all rows -- what a
-    # strided pass moving 16-column tiles cannot beat -- and the contiguous
-    # copy of a row pass
+    # copy of the same array in the column tiles of the plan's strided pass
+    # (the cluster tile width the plan reports, else 16 columns) over all
+    # rows -- what a strided pass moving such tiles cannot beat -- and the
+    # contiguous copy of a row pass
     ceiling = None
     full2 = wl["kind"] == "full" and len(shape) >= 2
     rowsv = wl["kind"] == "many" and len(shape) >= 2 and shape[-1] % 2 == 0
     if rank == 0 and headline and (full2 or rowsv) and elem == 8 and nlaunch:
         rows, cols = (shape[0], nelem // shape[0]) if full2 else (nelem // shape[-1], shape[-1])
+        mt = re.search(r"cluster-columns=(\d+)", plan.describe())
+        tile_w = int(mt.group(1)) if mt else 16
         gbs = {}
-        for w in ((16, cols) if full2 else (cols,)):
+        for w in ((tile_w, cols) if full2 else (cols,)):
             for _ in range(3):
                 L.check(lib.gbfft_probe_tile_copy(rows, cols, w, ctypes.c_void_p(x.data_ptr()),
                                                   ctypes.c_void_p(z.data_ptr()), sp), "gbfft_probe_tile_copy")
@@ -409,12 +413,13 @@ def measure_gbfft(args, wl, headline=True):
                 ts.append(a.elapsed_time(b))
             gbs[w] = bytes_pass / (statistics.median(ts) * 1e-3) / 1e9
         row_kernel = kernels[dom].startswith("row")
-        rel = gbs[cols] if row_kernel else gbs.get(16)
-        ceiling = {"kernel": kernels[dom], "tile16_copy_gbs": gbs.get(16), "contiguous_copy_gbs": gbs[cols],
+        rel = gbs[cols] if row_kernel else gbs.get(tile_w)
+        ceiling = {"kernel": kernels[dom], "tile_columns": tile_w if full2 else None,
+                   "tile_copy_gbs": gbs.get(tile_w) if full2 else None, "contiguous_copy_gbs": gbs[cols],
                    "frac_of_pattern": ach / rel if rel else None,
                    "note": "gbfft_probe_tile_copy over the %dx%d array: %s; frac_of_pattern = achieved / the "
                            "copy of the dominant kernel's pattern" % (
-                               rows, cols, "16-column tiles (the strided passes' pattern) and whole rows"
+                               rows, cols, "%d-column tiles (the strided pass's pattern) and whole rows" % tile_w
                                if full2 else "whole rows (the row kernels' pattern)")}
 
     # accuracy of one result vs FP64 (numpy pocketfft), outside the timed region

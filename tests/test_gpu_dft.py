@@ -110,6 +110,26 @@ def test_fused_shift_centre(gbfft_lib, shape, mode):
     plan.close()
 
 
+@pytest.mark.parametrize("colv", ["9", "16", "17", "18", "19"])
+def test_fused_shift_cluster_column_variants(gbfft_lib, monkeypatch, colv):
+    """The 4096-point cluster column kernels store the rotated output on their
+    own store path (scaled and conjugated for Inverse / Reverse): shift and
+    ishift stay bit-identical to shifting the plain result."""
+    g = gbfft_lib
+    monkeypatch.setenv("GBFFT_COL_VARIANT", colv)
+    rng = np.random.default_rng(72)
+    x = uniform_complex(rng, (4096, 4096), np.complex64)
+    xt = torch.from_numpy(x).cuda()
+    plan = g.Plan((4096, 4096), kind="full", dtype=torch.complex64)
+    for mode in ("forward", "inverse", "reverse"):
+        y = plan(mode, xt).cpu().numpy()
+        assert rel_l2(y, np_reference("fft2D", mode, x)) < 2e-6 * np.log2(x.size), (colv, mode)
+        assert np.array_equal(plan(mode, xt, shift_out="shift").cpu().numpy(), O.shift(y)), (colv, mode)
+        assert np.array_equal(plan(mode, xt, shift_out="ishift").cpu().numpy(), O.shift(y, inverse=True)), \
+            (colv, mode)
+    plan.close()
+
+
 @pytest.mark.parametrize("shape", [(7,), (5, 3), (3, 5, 7), (12, 9)])
 def test_fused_centre_odd_and_double(gbfft_lib, shape):
     """Odd extents: centring is not a rotation; the input pass runs first and

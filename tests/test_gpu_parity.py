@@ -344,7 +344,8 @@ def test_fault_injection_alloc(gbfft_lib, monkeypatch):
                                                ("", "1", "6"), ("", "1", "7"), ("", "1", "8"),
                                                ("", "1", "9"), ("", "1", "10"), ("", "1", "11"),
                                                ("", "1", "12"), ("", "1", "13"), ("", "1", "14"),
-                                               ("", "1", "15"), ("tma", "1", "14"), ("strided", "1", "9"),
+                                               ("", "1", "15"), ("", "1", "16"), ("", "1", "17"),
+                                               ("", "1", "18"), ("", "1", "19"), ("tma", "1", "14"), ("strided", "1", "9"),
                                                ("row", "1", "2"),
                                                ("cluster", "1", "2"), ("tma,row,cluster", "0", "0")])
 def test_kernel_variants_agree(gbfft_lib, monkeypatch, disable, rowv, colv):
