@@ -657,9 +657,13 @@ __device__ __forceinline__ void apply_table16(float2 (&v)[16], const float2* tab
   }
 }
 
+// twiddle table row pitch: 16 entries + one 16-byte pad, so the rows a warp
+// reads at once (four of t1, two of t2) start in different banks
+constexpr int kTabPitch = 18;
+
 template <int W>
 constexpr size_t col_r16b_smem() {
-  return size_t(512) * W * sizeof(float2) + size_t(512 + 256) * sizeof(float2);
+  return size_t(512) * W * sizeof(float2) + size_t(32 + 16) * kTabPitch * sizeof(float2);
 }
 
 template <int W, int MINB>
@@ -670,8 +674,8 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
   constexpr uint32_t kRecvBytes = 4096u * W / 8u * sizeof(C);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* rv = reinterpret_cast<C*>(smem_raw);  // [b][x][K1l], reused for the stage-2 exchange
-  C* t1 = rv + 512 * W;                     // [bl][K1]: W_4096^((32r + bl) * K1)
-  C* t2 = t1 + 512;                         // [gamma][kappa]: W_256^(gamma * kappa)
+  C* t1 = rv + 512 * W;                     // [bl][K1]: W_4096^((32r + bl) * K1), rows kTabPitch apart
+  C* t2 = t1 + 32 * kTabPitch;              // [gamma][kappa]: W_256^(gamma * kappa)
   __shared__ __align__(8) uint64_t rbar;
   const int r = int(cg::this_cluster().block_rank());
   const int64_t tile = int64_t(blockIdx.x) >> 3;
@@ -688,7 +692,9 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&rbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  cluster_arrive_release();
+  // the mbarrier init is published by its own release fence; the arrive only
+  // has to tell the siblings that this CTA runs
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
 
   // twiddle table entries first (their loads overlap the column loads).
   // Every table row is filled and read by the threads of one warp: row q of
@@ -717,15 +723,15 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
     }
   }
 #pragma unroll
-  for (int i = 0; i < 16 / W; ++i) t1[16 * q + x + W * i] = e1[i];
-  if (k2 < 16) t2[16 * (q >> 1) + k2] = e2;
+  for (int i = 0; i < 16 / W; ++i) t1[kTabPitch * q + x + W * i] = e1[i];
+  if (k2 < 16) t2[kTabPitch * (q >> 1) + k2] = e2;
   if (fl & F_CONJ_IN) {
 #pragma unroll
     for (int a = 0; a < 16; ++a) v[a].y = -v[a].y;
   }
   dft16(v);
   __syncwarp();  // this warp's twiddle table rows
-  apply_table16(v, t1 + 16 * q);  // W^(b*K1)
+  apply_table16(v, t1 + kTabPitch * q);  // W^(b*K1)
   if (tid == 0) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&rbar)),
                  "r"(kRecvBytes)
@@ -757,7 +763,7 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
 #pragma unroll
   for (int beta = 0; beta < 16; ++beta) v[beta] = col[(16 * beta + gamma) * 2 * W];
   dft16(v);
-  apply_table16(v, t2 + 16 * gamma);  // W_256^(gamma*kappa)
+  apply_table16(v, t2 + kTabPitch * gamma);  // W_256^(gamma*kappa)
   __syncthreads();  // every stage-2 read of the receive buffer is done
 #pragma unroll
   for (int kappa = 0; kappa < 16; ++kappa) col[(kappa * 16 + gamma) * 2 * W] = v[kappa];
@@ -903,8 +909,8 @@ struct ColR16TmaCfg {
   X(15, float, 8, 3)
 
 // lean radix-16 variants, Complex Float only (W, min CTAs per SM); 18 is the
-// default: on the 4096 x 4096 column pass 77.8 us against 86.0 us for 9
-// (16: 92.2, 19: 84.0-86.0, 10: 94.2, 8: 107.9)
+// default: on the 4096 x 4096 column pass 73.7 us against 86.0 us for 9
+// (16: 88.1, 19: 75.8-77.8, 17: 86.0, 10: 94.2, 8: 107.9)
 #define GBFFT_COLR16B_TABLE(X) \
   X(16, 16, 2)                 \
   X(17, 8, 5)                  \
