@@ -59,7 +59,7 @@ __device__ __forceinline__ void cluster_barrier() {
 __global__ void __cluster_dims__(kPCta, 1, 1) __launch_bounds__(kPThreads, 2) plane256_kernel(const PassDesc d) {
   extern __shared__ __align__(16) float2 psm[];
   float2* ex = psm;                     // row exchange [32][kPPitch], then receive buffer [256][32]
-  float2* wt = psm + kPRows * kPPitch;  // W_256^j
+  float2* wt = psm + kPRows * kPPitch;  // [k1][t]: W_256^(t*k1), t, k1 < 16 (t fastest: no bank conflicts)
   const uint32_t r = cg::this_cluster().block_rank();
   const int64_t plane = int64_t(blockIdx.x) / kPCta;
   const float2* __restrict__ in = static_cast<const float2*>(d.in) + plane * d.in_bs;
@@ -67,7 +67,7 @@ __global__ void __cluster_dims__(kPCta, 1, 1) __launch_bounds__(kPThreads, 2) pl
   const float2* __restrict__ tw = static_cast<const float2*>(d.tw);
   const uint32_t fl = d.flags;
   const int tid = threadIdx.x;
-  if (tid < kPN) wt[tid] = tw[tid];
+  if (tid < kPN) wt[tid] = tw[((tid & 15) * (tid >> 4)) & (kPN - 1)];
 
   // ---- row phase: thread (lr, t), row 32r + lr, elements t + 16i ---------------
   const int lr = tid >> 4, t = tid & 15;
@@ -84,7 +84,7 @@ __global__ void __cluster_dims__(kPCta, 1, 1) __launch_bounds__(kPThreads, 2) pl
   __syncthreads();  // twiddle table
   dft16(v);
 #pragma unroll
-  for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmul(v[k1], wt[(t * k1) & (kPN - 1)]);
+  for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmul(v[k1], wt[16 * k1 + t]);
   {
     float2* row = ex + lr * kPPitch;
 #pragma unroll
@@ -117,7 +117,7 @@ __global__ void __cluster_dims__(kPCta, 1, 1) __launch_bounds__(kPThreads, 2) pl
   __syncthreads();  // every read of the receive buffer is done before the exchange reuses it
   dft16(v);
 #pragma unroll
-  for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmul(v[k1], wt[(tc * k1) & (kPN - 1)]);
+  for (int k1 = 1; k1 < 16; ++k1) v[k1] = cmul(v[k1], wt[16 * k1 + tc]);
 #pragma unroll
   for (int k1 = 0; k1 < 16; ++k1) ex[(k1 * 16 + tc) * kPRows + c] = v[k1];
   __syncthreads();
