@@ -456,7 +456,7 @@ __device__ __forceinline__ void mma_f16_s(uint32_t tmem, uint64_t da, uint64_t d
       : "memory");
 }
 
-// d.tw: B tiles (kS_BBytes) followed by W_n^t, t < n (Complex Float);
+// d.tw: B tiles (kS_BBytes) followed by W_n^(j2*k1) at (k1 - 1)*n2 + j2 (Complex Float);
 // d.tc_nc = n2, d.tc_p = P2; rows d.ncols, strides in_cs / out_cs.
 __global__ void __launch_bounds__(kS_Threads, 2) tcdft8_kernel(const PassDesc d) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -560,18 +560,14 @@ __global__ void __launch_bounds__(kS_Threads, 2) tcdft8_kernel(const PassDesc d)
       }
       dft8(z0);
       dft8(z1);
-      // twiddle W_n^(j2*k1): indices stepped by j2 modulo n
+      // twiddle W_n^(j2*k1) from the table [k1 - 1][j2] (consecutive lanes,
+      // consecutive entries)
       {
         const int ja = one ? p : 0, jb = pair ? n2 - p : 0;
-        int ta = ja, tb = jb;
 #pragma unroll
         for (int k1 = 1; k1 < 8; ++k1) {
-          z0[k1] = cmul(z0[k1], Ws[ta]);
-          z1[k1] = cmul(z1[k1], Ws[tb]);
-          ta += ja;
-          ta -= (ta >= n) ? n : 0;
-          tb += jb;
-          tb -= (tb >= n) ? n : 0;
+          z0[k1] = cmul(z0[k1], Ws[(k1 - 1) * n2 + ja]);
+          z1[k1] = cmul(z1[k1], Ws[(k1 - 1) * n2 + jb]);
         }
       }
       // fold, split, store: quantity q = a, b, c, d; arrays 2q (hi) and 2q + 1
@@ -756,11 +752,14 @@ int tcdft8_add_pass(Builder& B, int64_t n, int64_t rows, int64_t in_cs, int64_t 
         std::memcpy(tb.data() + size_t(hh * 4 + 2 * u + 1) * kS_BTile + off, &lo, 2);
       }
     }
-  for (int64_t t = 0; t < n; ++t) {
-    const cd w = unit_root(t, n);
-    const float v[2] = {float(w.real()), float(w.imag())};
-    std::memcpy(tb.data() + kS_BBytes + size_t(t) * 8, v, 8);
-  }
+  // radix-8 twiddles W_n^(j2*k1) at (k1 - 1)*n2 + j2, k1 = 1..7, j2 < n2
+  // (7*n2 < n entries)
+  for (int k1 = 1; k1 < 8; ++k1)
+    for (int j2 = 0; j2 < n2; ++j2) {
+      const cd w = unit_root((int64_t(j2) * k1) % n, n);
+      const float v[2] = {float(w.real()), float(w.imag())};
+      std::memcpy(tb.data() + kS_BBytes + (size_t(k1 - 1) * size_t(n2) + size_t(j2)) * 8, v, 8);
+    }
   while (B.blob.size() % 256) B.blob.push_back(0);
   const size_t off = B.blob.size();
   B.blob.insert(B.blob.end(), tb.begin(), tb.end());
