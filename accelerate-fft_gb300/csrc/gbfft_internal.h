@@ -53,6 +53,7 @@ enum KernelId : int {
   K_TC_DFT = 6,   // split-FP16 dense DFT, step 2: tcgen05 GEMM against cos/sin tiles
   K_TC_DFT8 = 7,  // split-FP16 rows n = 8 * n2: radix-8 on the CUDA cores, dense n2 stage on tcgen05
   K_PLANE = 8,    // both axes of 256 x 256 planes in one pass (8-CTA cluster per plane)
+  K_VEC1024 = 9,  // one 1024-point Complex Double vector per 8-CTA cluster, one element per thread
 };
 
 struct StageInfo {
@@ -151,6 +152,8 @@ cudaError_t prepare_tcdft_kernels();
 bool plane_available(int64_t h, int64_t w, bool dbl);
 cudaError_t prepare_plane_kernels();
 cudaError_t launch_plane(const PassDesc& d, cudaStream_t s);
+bool vec1024_available(int64_t n, bool dbl);
+cudaError_t launch_vec1024(const PassDesc& d, cudaStream_t s);
 cudaError_t launch_tcdft(const PassDesc& d, cudaStream_t s);
 int col_tile_width(int variant);
 

@@ -63,6 +63,7 @@ const char* pass_kernel_name(const PassDesc& d, bool dbl) {
     case K_TC_DFT: return "tcdft_mma_kernel";
     case K_TC_DFT8: return "tcdft8_kernel";
     case K_PLANE: return "plane256_kernel";
+    case K_VEC1024: return "vec1024_kernel";
     case K_STRIDED: return str_kernel_name(d, dbl);
     default: return "pencil_kernel";
   }
@@ -75,6 +76,7 @@ cudaError_t launch_pass(const PassDesc& d, bool is_double, cudaStream_t stream) 
   if (d.kernel == K_STRIDED) return launch_str(d, is_double, stream);
   if (d.kernel == K_TC_FOLD || d.kernel == K_TC_DFT || d.kernel == K_TC_DFT8) return launch_tcdft(d, stream);
   if (d.kernel == K_PLANE) return launch_plane(d, stream);
+  if (d.kernel == K_VEC1024) return launch_vec1024(d, stream);
   const int grid = pass_grid(d);
   if (grid <= 0) return cudaSuccess;
   const size_t smem = pass_smem_bytes(d, is_double);

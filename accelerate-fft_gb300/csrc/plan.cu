@@ -439,6 +439,10 @@ static std::string radix_list(const PassDesc& d) {
   return r;
 }
 
+// Complex Double 1024-point vectors up to this many per axis run one per
+// 8-CTA cluster (vec1024.cu); more go to the throughput kernels.
+constexpr int64_t kVecMaxCols = 16;
+
 // Appends the passes of one axis.  `first`: this axis reads the user's
 // input; later axes work on the output buffer.
 int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool first,
@@ -467,7 +471,14 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     d.nbatch = d.nb_lo = ax.outer;
     choose_tile(ps, dbl);
     const char* kname = "pencil";
-    if (ax.es == 1 && ax.outer == 1 && use_row && row_kernel_available(int(ax.n), dbl) &&
+    if (ax.es == 1 && ax.outer == 1 && ax.ncols <= kVecMaxCols && vec1024_available(ax.n, dbl) &&
+        !feature_disabled("vec")) {
+      // a few Complex Double vectors of 1024: one cluster of 8 CTAs each,
+      // one element per thread (latency path)
+      d.kernel = K_VEC1024;
+      ps.tw_off = int64_t(B.roots_for(1024));
+      kname = "vec1024-cluster8";
+    } else if (ax.es == 1 && ax.outer == 1 && use_row && row_kernel_available(int(ax.n), dbl) &&
         !feature_disabled("row")) {
       d.kernel = K_ROW;
       kname = "row";

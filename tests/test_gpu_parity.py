@@ -144,6 +144,32 @@ def test_config1_fft1d_c64_roundtrip(gbfft_lib):
     assert rel_l2(xr, x) < 1e-14
 
 
+@pytest.mark.parametrize("rows", [1, 3, 16, 17])
+def test_c64_1024_vectors_cluster_path(gbfft_lib, rows):
+    """A few Complex Double vectors of 1024 run one per 8-CTA cluster
+    (vec1024_kernel, up to 16 vectors); 17 go to the throughput kernels.
+    Every mode against FP64, the fused shift (of the single-vector full plan)
+    bit-identical to shifting the plain result, and an input that the
+    transform may not modify."""
+    g = gbfft_lib
+    rng = np.random.default_rng(1000 + rows)
+    shape = (rows, 1024) if rows > 1 else (1024,)
+    x = uniform_complex(rng, shape, np.complex128)
+    t = torch.from_numpy(x).cuda()
+    plan = g.Plan(shape, kind="many" if rows > 1 else "full", dtype=torch.complex128)
+    assert ("vec1024_kernel" in plan.pass_kernels()) == (rows <= 16), plan.describe()
+    for mode in MODES:
+        y = plan(mode, t).cpu().numpy()
+        assert rel_l2(y, np_reference("fft", MODE_IDX[mode], x)) < 1e-14, (rows, mode)
+        if rows == 1:  # fused shifts are offered on full plans
+            assert np.array_equal(plan(mode, t, shift_out="shift").cpu().numpy(), O.shift(y)), mode
+            assert np.array_equal(plan(mode, t, shift_out="ishift").cpu().numpy(), O.shift(y, inverse=True)), mode
+    assert np.array_equal(t.cpu().numpy(), x)
+    from gbfft import _lib as L
+    assert L.lib().gbfft_exec_status(plan.handle, None) == 0
+    plan.close()
+
+
 # ---- reference properties (test/Test/FFT.hs:112-236) on the GPU -------------
 def _rev(x):
     n = x.shape[-1]
