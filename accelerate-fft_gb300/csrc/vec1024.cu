@@ -40,17 +40,33 @@ __device__ __forceinline__ double2 shfl_xor2(double2 v, int m) {
   return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
 }
 
+// The stage twiddles of one lane: tw[s] = W_{2h}^(lane mod h) for the stage
+// of half-size h = 16 >> s (W_{2h}^j = W_32^(j 16/h) = W_1024^(32 j 16/h)),
+// loaded once, before any is needed, and used by both DFTs of the lane.
+struct LaneTw {
+  double2 tw[4];
+};
+__device__ __forceinline__ LaneTw lane_twiddles(int lane, const double2* __restrict__ w1024) {
+  LaneTw t;
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int h = 16 >> s;
+    t.tw[s] = __ldg(w1024 + 32 * (lane & (h - 1)) * (16 / h));
+  }
+  return t;
+}
+
 // Radix-2 DIF DFT-32 across the lanes of a warp: lane l holds element l on
 // entry and output bitrev5(l) on return.  Stage with half-size h: the lower
 // lane of a pair keeps u + v, the upper (u - v) * W_{2h}^(l mod h).
-__device__ __forceinline__ double2 dft32_lanes(double2 x, int lane, const double2* __restrict__ w1024) {
+__device__ __forceinline__ double2 dft32_lanes(double2 x, int lane, const LaneTw& t) {
 #pragma unroll
-  for (int h = 16; h >= 1; h >>= 1) {
+  for (int s = 0; s < 5; ++s) {
+    const int h = 16 >> s;
     const double2 p = shfl_xor2(x, h);
     if (lane & h) {
       const double2 dlt = make_double2(p.x - x.x, p.y - x.y);
-      const int j = lane & (h - 1);
-      x = j ? cmul(dlt, __ldg(w1024 + 32 * j * (16 / h))) : dlt;  // W_{2h}^j = W_32^(j 16/h)
+      x = (s < 4 && (lane & (h - 1))) ? cmul(dlt, t.tw[s < 4 ? s : 0]) : dlt;
     } else {
       x = make_double2(x.x + p.x, x.y + p.y);
     }
@@ -75,12 +91,15 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(kVThreads) vec1024_k
 
   // ---- phase 1: warp b = 4r + warp, lane a -----------------------------------
   const int b = 4 * r + warp;
-  const double2* __restrict__ in = static_cast<const double2*>(d.in) + col * d.in_cs;
-  double2 x = in[32 * lane + b];
-  if (fl & F_CONJ_IN) x.y = -x.y;
-  x = dft32_lanes(x, lane, w);
   const int k1 = bitrev5(lane);
-  x = cmul(x, __ldg(w + ((b * k1) & (kVN - 1))));  // W_1024^(b k1)
+  const double2* __restrict__ in = static_cast<const double2*>(d.in) + col * d.in_cs;
+  // every load of the kernel is issued here, before any result is needed
+  double2 x = in[32 * lane + b];
+  const LaneTw lt = lane_twiddles(lane, w);
+  const double2 wb = __ldg(w + ((b * k1) & (kVN - 1)));  // W_1024^(b k1)
+  if (fl & F_CONJ_IN) x.y = -x.y;
+  x = dft32_lanes(x, lane, lt);
+  x = cmul(x, wb);
   if (tid == 0) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&rbar)), "r"(kVRecvBytes)
                  : "memory");
@@ -109,7 +128,7 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(kVThreads) vec1024_k
   if (!ok && d.status) atomicExch(d.status, GBFFT_ERR_TIMEOUT_DEVICE);
   const int kk1 = 4 * r + warp;
   double2 y = rv[warp * 32 + lane];
-  y = dft32_lanes(y, lane, w);
+  y = dft32_lanes(y, lane, lt);
   const int l = kk1 + 32 * bitrev5(lane);  // output index
   if (fl & F_SCALE) y = make_double2(y.x * d.scale, y.y * d.scale);
   if (fl & F_CONJ_OUT) y.y = -y.y;
