@@ -637,8 +637,8 @@ struct ColR16Cfg {
 //     being built by products of three table entries;
 //   * the two K1 values a thread sends to one CTA go as one 16-byte
 //     st.async (receive layout [b][x][K1l]), 8 pushes per thread instead of 16;
-//   * the flag handling (conjugation, scaling, output rotation, L2 hint) is
-//     hoisted out of the element loops into uniform branches.
+//   * the flag handling (conjugation, scaling, output rotation) is hoisted
+//     out of the element loops into uniform branches.
 __device__ __forceinline__ void st_async2(uint32_t addr, float2 a, float2 b, uint32_t bar) {
   asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
                    addr),
@@ -713,14 +713,11 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(32 * W, MINB)
   {
     const C* __restrict__ in = static_cast<const C*>(d.in) + bo * d.in_bs + x0 + int64_t(b) * d.in_es + x;
     const int64_t as = 256 * d.in_es;
-    if (fl & F_L2_IN_FIRST) {
-      const uint64_t pol = l2_policy_first();
+    // no evict-first hint on these loads: the other half of each 128-byte
+    // line is read by the neighbouring tile's cluster shortly after (with
+    // the hint the 4096 x 4096 column pass took 73.7 instead of 71.7 us)
 #pragma unroll
-      for (int a = 0; a < 16; ++a) v[a] = ld_l2hint(in + a * as, pol);
-    } else {
-#pragma unroll
-      for (int a = 0; a < 16; ++a) v[a] = in[a * as];
-    }
+    for (int a = 0; a < 16; ++a) v[a] = in[a * as];
   }
 #pragma unroll
   for (int i = 0; i < 16 / W; ++i) t1[kTabPitch * q + x + W * i] = e1[i];
