@@ -68,7 +68,7 @@ struct Builder {
 // on GB300 for fft2D 4096^2).
 struct TuneChoice {
   int row_variant = -1;  // contiguous rows: 1 single-buffered, 0 double-buffered, -1 by kernel
-  int row_tma = 0;      //   with row_variant 0: stream rows with cp.async.bulk
+  int row_tma = -1;     //   with row_variant 0: stream rows with cp.async.bulk (-1: by length)
   int col_variant = 18;  // 4096-point strided axes: cluster kernel variant (colfft.cu)
   int split_rank = 0;   // four-step axes: k-th best (n1, n2) factorisation
   int str_tma = 1;      // strided passes: tensor-copy-fed persistent kernel
