@@ -226,11 +226,6 @@ __device__ __forceinline__ void st_async(uint32_t addr, float2 v, uint32_t bar) 
                "f"(v.x), "f"(v.y), "r"(bar)
                : "memory");
 }
-__device__ __forceinline__ void st_async(uint32_t addr, double2 v, uint32_t bar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f64 [%0], {%1, %2}, [%3];" ::"r"(addr),
-               "d"(v.x), "d"(v.y), "r"(bar)
-               : "memory");
-}
 constexpr uint32_t kColWaitLimit = 1u << 22;
 
 template <typename T, int W, int U, int MINB>
