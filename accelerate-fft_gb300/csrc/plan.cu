@@ -472,7 +472,7 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
     choose_tile(ps, dbl);
     const char* kname = "pencil";
     if (ax.es == 1 && ax.outer == 1 && ax.ncols <= kVecMaxCols && vec1024_available(ax.n, dbl) &&
-        !feature_disabled("vec")) {
+        tc->row_kernel != 0 && !feature_disabled("vec")) {
       // a few Complex Double vectors of 1024: one cluster of 8 CTAs each,
       // one element per thread (latency path)
       d.kernel = K_VEC1024;

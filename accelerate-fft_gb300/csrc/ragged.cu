@@ -379,6 +379,8 @@ int create_ragged(gbfft_ragged_plan** out, int64_t count, const int64_t* lengths
     TuneChoice rc;
     rc.blue_pad = -1;  // the ragged executor's Bluestein weighting
     rc.blue_weight = rt.blue_weight;
+    rc.row_kernel = 0;  // passes run as generic or strided tiles below: no plan-only kernels
+                        // (register rows, the single-vector cluster kernel) and their tables
     const int st = add_axis(B, lc.passes, ax, true, s1, s2, desc, cap, &rc);
     if (st != GBFFT_OK) return st;
     lc.m = s2;  // rows (1) * m for the four-pass Bluestein, else 0

@@ -91,11 +91,13 @@ def test_ragged_dependency_wait_times_out(gbfft_lib, monkeypatch):
 
 
 def test_ragged_offsets_with_gaps_and_double(gbfft_lib):
+    # (1024 and 4096 in Complex Double: lengths the plans run on kernels of
+    # their own, which the ragged executor replaces by its tiles)
     g = gbfft_lib
-    lengths = np.array([16, 1000, 1009, 5, 8192, 3], np.int64)
-    modes = np.array([-1, 2, 1, -1, 2, 1], np.int32)
-    offsets = np.array([0, 40, 1100, 3000, 3020, 12000], np.int64)
-    total = 12010
+    lengths = np.array([16, 1000, 1009, 5, 8192, 3, 1024, 4096], np.int64)
+    modes = np.array([-1, 2, 1, -1, 2, 1, 2, -1], np.int32)
+    offsets = np.array([0, 40, 1100, 3000, 3020, 12000, 12010, 13100], np.int64)
+    total = 17200
     rng = np.random.default_rng(1)
     x = (rng.standard_normal(total) + 1j * rng.standard_normal(total)).astype(np.complex128)
     plan = g.RaggedPlan(lengths, modes, offsets=offsets, dtype=torch.complex128)
