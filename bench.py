@@ -170,7 +170,7 @@ for _name, _wl in WORKLOADS.items():
 # below the algorithmic bytes.  The ragged figure is the 2000-transform
 # capture scaled by elements (same length distribution, traffic proportional).
 NCU_TRAFFIC = {
-    "fft2d_4096": ("colfft4096_r16_kernel", 134271232 + 73015296),
+    "fft2d_4096": ("colfft4096_r16b_kernel", 134282496 + 78467072),
     "fft3d_256": ("strfft_tma_kernel", 134264320 + 51690752),
     "ragged_20000": ("ragged_kernel", 1.0691e9 * 157602267 / 16295261),
     "ragged_2000": ("ragged_kernel", 1.0691e9),
