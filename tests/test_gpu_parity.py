@@ -170,6 +170,28 @@ def test_c64_1024_vectors_cluster_path(gbfft_lib, rows):
     plan.close()
 
 
+@pytest.mark.parametrize("shape,dt", [((8192, 64), np.complex64), ((8192, 24), np.complex64),
+                                      ((3, 8192, 16), np.complex64), ((6144, 16), np.complex64),
+                                      ((3000, 16), np.complex64)])
+def test_long_strided_axes_four_step(gbfft_lib, shape, dt):
+    """Strided axes longer than 2048 without a strided kernel of their own
+    (8192, 6144, 3000) run as two four-step passes instead of one generic
+    tile holding one or two columns; every mode against FP64."""
+    g = gbfft_lib
+    rng = np.random.default_rng(sum(shape))
+    x = uniform_complex(rng, shape, dt)
+    plan = g.Plan(shape, kind="full", dtype=torch.complex64 if dt == np.complex64 else torch.complex128)
+    assert "four-step" in plan.describe(), plan.describe()
+    xt = torch.from_numpy(x).cuda()
+    fam = {2: "fft2D", 3: "fft3D"}[len(shape)]
+    for mode in MODES:
+        y = plan(mode, xt).cpu().numpy()
+        assert rel_l2(y, np_reference(fam, MODE_IDX[mode], x)) < tol_fp64(dt, shape), (shape, mode)
+    from gbfft import _lib as L
+    assert L.lib().gbfft_exec_status(plan.handle, None) == 0
+    plan.close()
+
+
 # ---- reference properties (test/Test/FFT.hs:112-236) on the GPU -------------
 def _rev(x):
     n = x.shape[-1]
