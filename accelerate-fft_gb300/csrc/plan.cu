@@ -461,18 +461,24 @@ int add_axis(Builder& B, std::vector<PassSpec>& passes, const Axis& ax, bool fir
   if (ax.n <= 1) return GBFFT_OK;
 
   // A long strided axis (columns of a 2-D array, middle / outer axes of 3-D)
-  // with no strided kernel of its own goes four-step above 2048: in one
-  // generic tile it would hold only one or two columns and read short row
-  // segments (fft2D 8192^2: 1.65 ms that way, 0.68 ms four-step with both
-  // halves on the strided kernels).  2048 stays one pass: its four-step
-  // split has a 32-point generic half and measured no faster (0.085 ms
-  // against 0.083 ms for fft2D 2048^2).
+  // with no strided kernel of its own goes four-step above 2048 when a half
+  // of the split has a strided kernel: in one generic tile it would hold
+  // only one or two columns and read short row segments (fft2D 8192^2: 1.65
+  // ms that way, 0.68 ms four-step with both halves on the strided kernels;
+  // 6144^2: 1.17 -> 0.98 ms with one).  With two generic halves the split
+  // measured slower (3000^2: 0.36 against 0.30 ms), and 2048 (a 32-point
+  // generic half) no faster, so those stay one pass.
   const bool own_strided_kernel =
       ax.cs == 1 && ((ax.n == 4096 && ax.ncols % (dbl ? 16 : 8) == 0 && !feature_disabled("cluster")) ||
                      (str_kernel_available(int(ax.n), dbl) && ax.ncols % str_kernel_width(dbl) == 0 &&
                       !feature_disabled("strided")));
-  const bool long_strided = ax.es != 1 && ax.n > 2048 && ax.cs == 1 && ax.ncols == ax.es &&
-                            !own_strided_kernel && !feature_disabled("longcol");
+  bool long_strided = ax.es != 1 && ax.n > 2048 && ax.cs == 1 && ax.ncols == ax.es && is_fast_length(ax.n) &&
+                      !own_strided_kernel && !feature_disabled("longcol");
+  if (long_strided) {
+    int64_t h1 = 0, h2 = 0;
+    long_strided = split_four_step(ax.n, cap, h1, h2, dbl, split_rank) &&
+                   (str_kernel_available(int(h1), dbl) || str_kernel_available(int(h2), dbl));
+  }
 
   if (is_fast_length(ax.n) && ax.n <= cap && !long_strided) {
     PassSpec ps = blank_pass();

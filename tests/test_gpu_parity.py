@@ -170,18 +170,19 @@ def test_c64_1024_vectors_cluster_path(gbfft_lib, rows):
     plan.close()
 
 
-@pytest.mark.parametrize("shape,dt", [((8192, 64), np.complex64), ((8192, 24), np.complex64),
-                                      ((3, 8192, 16), np.complex64), ((6144, 16), np.complex64),
-                                      ((3000, 16), np.complex64)])
-def test_long_strided_axes_four_step(gbfft_lib, shape, dt):
+@pytest.mark.parametrize("shape,dt,split", [((8192, 64), np.complex64, True), ((8192, 24), np.complex64, True),
+                                            ((3, 8192, 16), np.complex64, True), ((6144, 16), np.complex64, True),
+                                            ((3000, 16), np.complex64, False)])
+def test_long_strided_axes_four_step(gbfft_lib, shape, dt, split):
     """Strided axes longer than 2048 without a strided kernel of their own
-    (8192, 6144, 3000) run as two four-step passes instead of one generic
-    tile holding one or two columns; every mode against FP64."""
+    run as two four-step passes when a half of the split has a strided
+    kernel (8192 = 64 x 128, 6144 = 64 x 96) and as one generic pass
+    otherwise (3000 = 50 x 60); every mode against FP64."""
     g = gbfft_lib
     rng = np.random.default_rng(sum(shape))
     x = uniform_complex(rng, shape, dt)
     plan = g.Plan(shape, kind="full", dtype=torch.complex64 if dt == np.complex64 else torch.complex128)
-    assert "four-step" in plan.describe(), plan.describe()
+    assert ("four-step" in plan.describe()) == split, plan.describe()
     xt = torch.from_numpy(x).cuda()
     fam = {2: "fft2D", 3: "fft3D"}[len(shape)]
     for mode in MODES:
