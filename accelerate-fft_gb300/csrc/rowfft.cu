@@ -667,10 +667,12 @@ int RowCfg<T, N, E, ROWS, MINB, Rs...>::tma_ctas_per_sm = 1;
 // radices = factor_device(N)).  Rows per CTA are chosen small and CTAs per
 // SM high, so some CTAs load while others compute: measured on GB300 with
 // the double-buffered kernel (milliseconds for 512 MiB of rows),
+//   128: 16 rows x 5 CTAs (before: the generic tile)
 //   256: 16 rows x 3 CTAs 0.169, 8 x 5 0.161    512: 0.187 -> 0.177
 //  1024: 0.201 -> 0.189                        2048: 0.210 -> 0.191
 //  1000 (100 threads a row): 4 rows x 2 CTAs 0.251, 2 x 5 (56 registers) 0.203.
 #define GBFFT_ROW_TABLE(X)                   \
+  X(float, 128, 16, 16, 5, 16, 8)            \
   X(float, 256, 16, 8, 5, 16, 16)            \
   X(float, 512, 16, 4, 5, 16, 16, 2)         \
   X(float, 1024, 16, 2, 5, 16, 16, 4)        \
