@@ -667,11 +667,15 @@ int RowCfg<T, N, E, ROWS, MINB, Rs...>::tma_ctas_per_sm = 1;
 // radices = factor_device(N)).  Rows per CTA are chosen small and CTAs per
 // SM high, so some CTAs load while others compute: measured on GB300 with
 // the double-buffered kernel (milliseconds for 512 MiB of rows),
-//   128: 16 rows x 5 CTAs (before: the generic tile)
+//    32, 64, 128 (64, 32, 16 rows x 5 CTAs; before: the generic tile): 1M rows
+//   of 128 1.28 -> 0.31 ms, 2M rows of 64 1.26 -> 0.44 ms, 4M rows of 32
+//   1.26 -> 0.82 ms
 //   256: 16 rows x 3 CTAs 0.169, 8 x 5 0.161    512: 0.187 -> 0.177
 //  1024: 0.201 -> 0.189                        2048: 0.210 -> 0.191
 //  1000 (100 threads a row): 4 rows x 2 CTAs 0.251, 2 x 5 (56 registers) 0.203.
 #define GBFFT_ROW_TABLE(X)                   \
+  X(float, 32, 16, 64, 5, 16, 2)             \
+  X(float, 64, 16, 32, 5, 16, 4)             \
   X(float, 128, 16, 16, 5, 16, 8)            \
   X(float, 256, 16, 8, 5, 16, 16)            \
   X(float, 512, 16, 4, 5, 16, 16, 2)         \
